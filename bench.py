@@ -1,0 +1,369 @@
+"""Benchmark of the batched FP32 tridiagonal solve on GB300.
+
+Workload (one "step"): one solve of the large fixed-size FP32 batch,
+65536 independent systems x 256 unknowns, contiguous per-system layout,
+seeded strictly diagonally dominant inputs (a, c ~ U[-1,1], a[0] = c[n-1] = 0,
+b = |a|+|c|+U[1,2], d ~ U[-1,1]), solved by cyclic reduction (cr).  The
+inputs (4 x 64 MiB) are larger than the 129 MB L2, so nothing is flushed
+between steps.  Metric: unknowns solved per second; the roofline is the HBM
+bandwidth at 20 algorithmic bytes per unknown (a, b, c, d read, x written).
+
+Lines printed (rank 0, one JSON line):
+  * value: device-resident throughput (CUDA events around K back-to-back
+    steps on the launching stream, max over ranks);
+  * e2e: the same through the reference-facing host-pointer launcher
+    (tridi_dropin_solve_f32 = cr()), pinned host buffers, host<->device copies
+    inside the timed region;
+  * roofline, cpu_baseline, clocks, per-kernel table (cr, crNBC, pcr, crpcr
+    over its switch levels) for the same batch.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference's own CPU gold solver (the oracle's
+restatement of tridiagonal_gold.h, bit-identical to it) on every host core,
+on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+M, N = 65536, 256
+BYTES_PER_UNKNOWN = 20  # a, b, c, d in + x out, FP32
+METRIC = "unknowns/s"
+WORKLOAD = "batched FP32 tridiagonal solve, 65536 systems x 256 unknowns, contiguous"
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "cr_65536x256_ncu.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            f = [v.strip() for v in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_init(gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if os.environ.get("TRIDI_BENCH_GLOO") != "1" else "gloo")
+    return rank, local, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v: float, world: int, device) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+def cpu_gold_rate(a, b, c, d, threads: int, min_seconds: float = 10.0):
+    """Times the oracle's gold Thomas (tridiagonal_gold.h:26-53, restated in
+    oracle/gold.c) on `threads` host threads over repetitions of the batch."""
+    from oracle import gold
+
+    gold.gold_lib()
+    x = gold.serial_many(a[:64], b[:64], c[:64], d[:64], threads=threads)  # warm up
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        x = gold.serial_many(a, b, c, d, threads=threads)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds or reps >= 200:
+            break
+    unknowns = reps * a.size
+    return unknowns / el, reps, el
+
+
+def run_reference(args):
+    rank, local, world = dist_init(args.gpus)
+    if rank != 0:
+        return 0
+    from oracle import gold
+    from tridiagonalsolvers_gb300 import workloads
+
+    cores = gold.gold_lib().gold_max_threads()
+    sample_m = 16384  # a quarter of the batch per step keeps each step ~0.1-1 s
+    a, b, c, d = workloads.dominant(sample_m, N, seed=workloads.SEEDS["c2"])
+    for _ in range(max(args.warmup, 0)):
+        gold.serial_many(a, b, c, d, threads=cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gold.serial_many(a, b, c, d, threads=cores)
+    el = time.perf_counter() - t0
+    rate = args.steps * a.size / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "unknowns/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_systems_per_step": sample_m, "system_size": N},
+        "cpu_baseline": {"value": rate, "unit": "unknowns/s", "cores": cores, "kind": "port",
+                         "sample": f"{sample_m} of the {M} systems per step (gold Thomas, FP32, OpenMP over systems)"},
+        "e2e": {"value": rate, "unit": "unknowns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def time_kernel(fn, stream, warmup, iters):
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(iters):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / iters
+
+
+def run_gpu(args):
+    import torch
+
+    import tridiagonalsolvers_gb300 as tg
+    from tridiagonalsolvers_gb300 import _lib, workloads
+
+    rank, local, world = dist_init(args.gpus)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.lib()
+    stream = torch.cuda.current_stream(dev)
+
+    a, b, c, d = workloads.dominant(M, N, seed=workloads.SEEDS["c2"] + rank)
+    ta, tb, tc, td = (torch.from_numpy(v).to(dev) for v in (a, b, c, d))
+    tx = torch.empty_like(ta)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    ptrs = [t.data_ptr() for t in (ta, tb, tc, td, tx)]
+
+    def step():
+        _lib.check(lib.tridi_cr_f32(*ptrs, N, M, sp), "tridi_cr_f32")
+
+    # correctness guard on a sample (the timed numbers are meaningless otherwise)
+    step()
+    torch.cuda.synchronize()
+    if rank == 0:
+        from oracle import gold
+
+        xs = tx[:32].cpu().numpy()
+        res = gold.rel_residual(a[:32], b[:32], c[:32], d[:32], xs).max()
+        if not res < 2e-6:
+            raise SystemExit(f"bench: cr result fails the oracle check (residual {res:.2e})")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier(world)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(ms, world, dev)
+    status = tg.device_status()
+    unknowns = M * N
+    value = world * unknowns / (ms * 1e-3)
+
+    # ---- end to end through the host-pointer launcher (reference-facing cr()) ----
+    ha, hb, hc, hd = (torch.from_numpy(v).pin_memory() for v in (a, b, c, d))
+    hx = torch.empty_like(ha).pin_memory()
+    hptrs = [t.data_ptr() for t in (ha, hb, hc, hd, hx)]
+
+    def e2e_step():
+        _lib.check(lib.tridi_dropin_solve_f32(0, *hptrs, N, M, 0), "tridi_dropin_solve_f32")
+
+    e2e_steps = max(2, min(args.steps, 10))
+    for _ in range(2):
+        e2e_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    barrier(world)
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world, dev)
+    if rank == 0:
+        from oracle import gold
+
+        res = gold.rel_residual(a[:32], b[:32], c[:32], d[:32], hx[:32].numpy()).max()
+        if not res < 2e-6:
+            raise SystemExit(f"bench: drop-in cr result fails the oracle check (residual {res:.2e})")
+
+    # ---- per-kernel table on the same batch (outside the timed region) ----
+    peak, peak_kind = measured_peaks()
+    kernels = {}
+    if rank == 0 and not args.no_table:
+        cands = [("cr", lambda: lib.tridi_cr_f32(*ptrs, N, M, sp)),
+                 ("crNBC", lambda: lib.tridi_cr_nbc_f32(*ptrs, N, M, sp)),
+                 ("pcr", lambda: lib.tridi_pcr_f32(*ptrs, N, M, sp))]
+        rest = 2
+        while rest <= N // 2:
+            cands.append((f"crpcr_rest{rest}", (lambda r: lambda: lib.tridi_crpcr_f32(*ptrs, N, M, r, sp))(rest)))
+            rest *= 2
+        for name, fn in cands:
+            t = time_kernel(fn, stream, 3, 20)
+            gbs = BYTES_PER_UNKNOWN * unknowns / (t * 1e-3) / 1e9
+            kernels[name] = {"ms": round(t, 5), "unknowns_per_s": unknowns / (t * 1e-3), "gbs": round(gbs, 1),
+                             "frac": round(gbs / peak, 4)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import gold
+
+        cores = gold.gold_lib().gold_max_threads()
+        sm = 8192
+        rate, reps, el = cpu_gold_rate(a[:sm], b[:sm], c[:sm], d[:sm], cores, min_seconds=3.0)
+        cpu = {"value": rate, "unit": "unknowns/s", "cores": cores, "kind": "port",
+               "sample": f"{reps} x {sm} of the {M} systems (gold Thomas FP32, {el:.1f} s wall on {cores} threads)"}
+
+    if rank == 0:
+        achieved = BYTES_PER_UNKNOWN * unknowns / (ms * 1e-3) / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": "unknowns/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "num_systems": M, "system_size": N, "solver": "cr",
+                       "layout": "contiguous", "l2": "inputs (256 MiB) larger than L2, no flush",
+                       "seed": workloads.SEEDS["c2"], "parallelism": f"replicas x{world} (independent batches)"},
+            "e2e": {"value": world * unknowns / e2e_s, "unit": "unknowns/s",
+                    "h2d_bytes_per_step": 4 * unknowns * 4, "d2h_bytes_per_step": unknowns * 4,
+                    "path": "tridi_dropin_solve_f32 (cr() drop-in), pinned host buffers"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": profile_traffic(), "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": BYTES_PER_UNKNOWN * unknowns},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps,
+            "device_status": status,
+            "kernels": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--no-table", action="store_true", help="skip the per-kernel table")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "native":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,106 @@
+/*
+ * tridi.h -- C ABI of the GB300-native batched tridiagonal solvers.
+ *
+ * Every entry point here is extern "C", takes plain pointers and sizes, and is
+ * what a foreign-function binding (ctypes, cgo, JNI, ...) or the C++ drop-in
+ * launchers of tridi_dropin.h call.  System i of a batch is
+ *
+ *     a[k] x[k-1] + b[k] x[k] + c[k] x[k+1] = d[k],   k = 0 .. n-1,
+ *
+ * with a[0] and c[n-1] ignored as zero (the reference assumes a[0] = c[n-1] =
+ * 0).  Unless stated otherwise the layout is contiguous per system: element k
+ * of system s is at s*n + k, as in every reference kernel (cr_kernel.cu:26).
+ *
+ * Conventions of the device-pointer API (tridi_*_f32 / _f64):
+ *   - a, b, c, d, x are DEVICE pointers, 16-byte aligned (cudaMalloc memory
+ *     is); a, b, c, d are read only (the reference kernels overwrite them);
+ *     x receives the solution and must not alias the inputs.
+ *   - Calls are asynchronous on `stream` (a cudaStream_t / CUstream; NULL is
+ *     the legacy default stream) and allocate nothing, except that the first
+ *     call on a device allocates that device's 64-byte status word; call
+ *     tridi_init() first to do that outside of stream capture.
+ *   - Status codes are returned instead of the reference's print-and-exit
+ *     (CUDA_SAFE_CALL).  A bounded device-side wait that runs out is not seen
+ *     by the call that launched it; tridi_device_status() reports it.
+ */
+#ifndef TRIDI_H
+#define TRIDI_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tridi_status {
+  TRIDI_SUCCESS = 0,
+  TRIDI_ERROR_INVALID_VALUE = 1,     /* null pointer, negative or zero count, bad enum */
+  TRIDI_ERROR_UNSUPPORTED_SIZE = 2,  /* system size outside the solver's range */
+  TRIDI_ERROR_MISALIGNED = 3,        /* a pointer is not 16-byte aligned */
+  TRIDI_ERROR_CUDA = 4,              /* a CUDA call failed: tridi_last_cuda_error() */
+  TRIDI_ERROR_DEVICE_TIMEOUT = 5,    /* a bounded device wait ran out */
+  TRIDI_ERROR_NOT_CONVERGED = 6,     /* iterative refinement hit its sweep limit */
+  TRIDI_ERROR_OUT_OF_MEMORY = 7,     /* admission or allocation refused */
+  TRIDI_ERROR_WORKSPACE_TOO_SMALL = 8,
+  TRIDI_ERROR_BUSY = 9               /* a bounded host-side queue is full */
+} tridi_status;
+
+/* Bits of the per-device status word (tridi_device_status). */
+#define TRIDI_DEVERR_WAIT_TIMEOUT 0x1u /* an mbarrier / flag wait exceeded its limit */
+
+typedef void *tridi_stream_t; /* cudaStream_t */
+
+/* ---- library ------------------------------------------------------------ */
+const char *tridi_version(void);
+const char *tridi_status_string(tridi_status s);
+/* The cudaError_t of the last TRIDI_ERROR_CUDA on this thread (0 if none). */
+int tridi_last_cuda_error(void);
+/* Allocates the current device's status word (done lazily otherwise). */
+tridi_status tridi_init(void);
+/* Synchronises the device, returns the OR of all TRIDI_DEVERR_* bits raised on
+   the current device since the last reset, and clears them when reset != 0. */
+tridi_status tridi_device_status(unsigned *bits, int reset);
+
+/* ---- the reference's solvers, device pointers ---------------------------- */
+/* Cyclic reduction.  Replaces cr() of cr_app.cu:4 / crKernel (cr_kernel.cu:1).
+   n a power of two, 2 <= n <= 8192. */
+tridi_status tridi_cr_f32(const float *a, const float *b, const float *c, const float *d, float *x, int n,
+                          int num_systems, tridi_stream_t stream);
+tridi_status tridi_cr_f64(const double *a, const double *b, const double *c, const double *d, double *x,
+                          int n, int num_systems, tridi_stream_t stream);
+
+/* Parallel cyclic reduction.  Replaces pcr() of pcr_app.cu:5 / pcrKernel
+   (pcr_kernel.cu:1).  n a power of two, 2 <= n <= 4096. */
+tridi_status tridi_pcr_f32(const float *a, const float *b, const float *c, const float *d, float *x, int n,
+                           int num_systems, tridi_stream_t stream);
+tridi_status tridi_pcr_f64(const double *a, const double *b, const double *c, const double *d, double *x,
+                           int n, int num_systems, tridi_stream_t stream);
+
+/* Hybrid CR -> PCR -> CR with switch level `rest_system_size` (the size of the
+   intermediate system solved by PCR: a power of two, 2 <= rest <= n/2).
+   Replaces crpcr() of crpcr_app.cu:5 / crpcrKernel (crpcr_kernel.cu:1). */
+tridi_status tridi_crpcr_f32(const float *a, const float *b, const float *c, const float *d, float *x, int n,
+                             int num_systems, int rest_system_size, tridi_stream_t stream);
+tridi_status tridi_crpcr_f64(const double *a, const double *b, const double *c, const double *d, double *x,
+                             int n, int num_systems, int rest_system_size, tridi_stream_t stream);
+
+/* Bank-conflict-free shared-memory cyclic reduction.  Replaces crNBC()
+   (crNBC.cu:123 / crNBCKernel :20) and crNBC32() (crNBC32banks.cu:123 /
+   crNBC32Kernel :20).  n a power of two, 2 <= n <= 2048. */
+tridi_status tridi_cr_nbc_f32(const float *a, const float *b, const float *c, const float *d, float *x, int n,
+                              int num_systems, tridi_stream_t stream);
+tridi_status tridi_cr_nbc_f64(const double *a, const double *b, const double *c, const double *d, double *x,
+                              int n, int num_systems, tridi_stream_t stream);
+
+/* Hybrid with the bank-conflict-free CR part.  Replaces crpcrNBC()
+   (crNBC.cu:344 / crpcrNBCKernel :189). */
+tridi_status tridi_crpcr_nbc_f32(const float *a, const float *b, const float *c, const float *d, float *x,
+                                 int n, int num_systems, int rest_system_size, tridi_stream_t stream);
+tridi_status tridi_crpcr_nbc_f64(const double *a, const double *b, const double *c, const double *d,
+                                 double *x, int n, int num_systems, int rest_system_size,
+                                 tridi_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TRIDI_H */

@@ -1,0 +1,60 @@
+// Algorithm dispatch of the host-pointer drop-ins onto the device-pointer C
+// ABI, and the scratch each algorithm needs.
+#include "runtime.h"
+#include "tridi.h"
+#include "tridi_dropin.h"
+
+namespace tridi {
+
+namespace {
+template <class T>
+struct Abi;
+template <>
+struct Abi<float> {
+  static constexpr auto cr = tridi_cr_f32;
+  static constexpr auto pcr = tridi_pcr_f32;
+  static constexpr auto crpcr = tridi_crpcr_f32;
+  static constexpr auto cr_nbc = tridi_cr_nbc_f32;
+  static constexpr auto crpcr_nbc = tridi_crpcr_nbc_f32;
+};
+template <>
+struct Abi<double> {
+  static constexpr auto cr = tridi_cr_f64;
+  static constexpr auto pcr = tridi_pcr_f64;
+  static constexpr auto crpcr = tridi_crpcr_f64;
+  static constexpr auto cr_nbc = tridi_cr_nbc_f64;
+  static constexpr auto crpcr_nbc = tridi_crpcr_nbc_f64;
+};
+}  // namespace
+
+template <class T>
+size_t algo_scratch_bytes(int algo, int n, int m, int param) {
+  (void)algo; (void)n; (void)m; (void)param;
+  return 0;
+}
+
+template <class T>
+tridi_status dropin_device_solve(int algo, const T* a, const T* b, const T* c, const T* d, T* x, int n, int m,
+                                 int param, void* ws, size_t ws_bytes, cudaStream_t s) {
+  (void)ws; (void)ws_bytes;
+  tridi_stream_t st = reinterpret_cast<tridi_stream_t>(s);
+  switch (algo) {
+    case TRIDI_DROPIN_CR: return Abi<T>::cr(a, b, c, d, x, n, m, st);
+    case TRIDI_DROPIN_PCR: return Abi<T>::pcr(a, b, c, d, x, n, m, st);
+    case TRIDI_DROPIN_CRPCR: return Abi<T>::crpcr(a, b, c, d, x, n, m, param, st);
+    case TRIDI_DROPIN_CR_NBC:
+    case TRIDI_DROPIN_CR_NBC32: return Abi<T>::cr_nbc(a, b, c, d, x, n, m, st);
+    case TRIDI_DROPIN_CRPCR_NBC: return Abi<T>::crpcr_nbc(a, b, c, d, x, n, m, param, st);
+    default: return TRIDI_ERROR_INVALID_VALUE;
+  }
+}
+
+template size_t algo_scratch_bytes<float>(int, int, int, int);
+template size_t algo_scratch_bytes<double>(int, int, int, int);
+template tridi_status dropin_device_solve<float>(int, const float*, const float*, const float*, const float*,
+                                                 float*, int, int, int, void*, size_t, cudaStream_t);
+template tridi_status dropin_device_solve<double>(int, const double*, const double*, const double*,
+                                                  const double*, double*, int, int, int, void*, size_t,
+                                                  cudaStream_t);
+
+}  // namespace tridi

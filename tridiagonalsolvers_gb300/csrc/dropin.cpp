@@ -1,0 +1,226 @@
+// The reference's host launchers (include/tridi_dropin.h) on the GB300
+// kernels.  Host pointers in, host pointers out, synchronous.
+//
+// Per call: the batch is cut into chunks of whole systems; chunk i is copied
+// host->device, solved and copied back on stream i % 2, so the copies of one
+// chunk overlap the solve of another and host->device overlaps device->host.
+// Device buffers come from a persistent per-device workspace (grown on
+// demand, never shrunk until tridi_dropin_release), not from a cudaMalloc
+// and cudaFree per call as in cr_app.cu:20-24,61-65.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "runtime.h"
+#include "tridi.h"
+#include "tridi_dropin.h"
+
+namespace tridi {
+
+// Device work of one chunk (implemented by the kernel translation units).
+template <class T>
+tridi_status dropin_device_solve(int algo, const T* a, const T* b, const T* c, const T* d, T* x, int n, int m,
+                                 int param, void* ws, size_t ws_bytes, cudaStream_t s);
+
+namespace {
+
+struct Workspace {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  cudaStream_t stream[2] = {nullptr, nullptr};
+};
+constexpr int kMaxDev = 64;
+Workspace g_ws[kMaxDev];
+std::mutex g_mu;
+
+cudaError_t ensure_workspace(Workspace& w, size_t bytes) {
+  cudaError_t e;
+  if (!w.stream[0]) {
+    for (auto& s : w.stream)
+      if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) return e;
+  }
+  if (w.bytes >= bytes) return cudaSuccess;
+  if (w.ptr) {
+    cudaStreamSynchronize(w.stream[0]);
+    cudaStreamSynchronize(w.stream[1]);
+    cudaFree(w.ptr);
+    w.ptr = nullptr;
+    w.bytes = 0;
+  }
+  if ((e = cudaMalloc(&w.ptr, bytes)) != cudaSuccess) return e;
+  w.bytes = bytes;
+  return cudaSuccess;
+}
+
+size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+// Extra device scratch the algorithm needs for m systems of size n.
+template <class T>
+size_t algo_scratch(int algo, int n, int m, int param);
+
+template <class T>
+tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d, T* x, int n, int m, int param) {
+  if (!a || !b || !c || !d || !x || n <= 0 || m <= 0) return TRIDI_ERROR_INVALID_VALUE;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (dev < 0 || dev >= kMaxDev) return TRIDI_ERROR_INVALID_VALUE;
+  std::lock_guard<std::mutex> lock(g_mu);
+  Workspace& w = g_ws[dev];
+
+  // Chunks of about 32 MiB of input (8 MiB per coefficient array), whole
+  // systems, at most 16 chunks.
+  const size_t sys_bytes = (size_t)n * sizeof(T);
+  long per = (long)((8u << 20) / sys_bytes);
+  if (per < 1) per = 1;
+  if (per * 16 < m) per = (m + 15) / 16;
+  if (per > m) per = m;
+  const size_t arr = align256((size_t)m * sys_bytes);
+  const size_t scratch = align256(algo_scratch<T>(algo, n, m, param));
+  if ((e = ensure_workspace(w, 5 * arr + scratch)) != cudaSuccess) return cuda_status(e);
+  char* base = static_cast<char*>(w.ptr);
+  T* da = reinterpret_cast<T*>(base);
+  T* db = reinterpret_cast<T*>(base + arr);
+  T* dc = reinterpret_cast<T*>(base + 2 * arr);
+  T* dd = reinterpret_cast<T*>(base + 3 * arr);
+  T* dx = reinterpret_cast<T*>(base + 4 * arr);
+  void* ws = base + 5 * arr;
+
+  tridi_status st = TRIDI_SUCCESS;
+  for (long s0 = 0, k = 0; s0 < m; s0 += per, ++k) {
+    const long cnt = (m - s0) < per ? (m - s0) : per;
+    const size_t off = (size_t)s0 * n, bytes = (size_t)cnt * sys_bytes;
+    cudaStream_t s = w.stream[k & 1];
+    if ((e = cudaMemcpyAsync(da + off, a + off, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(db + off, b + off, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dc + off, c + off, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dd + off, d + off, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess) {
+      st = cuda_status(e);
+      break;
+    }
+    // Chunks use disjoint slices of the scratch: give each its share.
+    const size_t ws_share = scratch / ((m + per - 1) / per);
+    st = dropin_device_solve<T>(algo, da + off, db + off, dc + off, dd + off, dx + off, n, (int)cnt, param,
+                                static_cast<char*>(ws) + (size_t)k * (ws_share & ~size_t(255)),
+                                ws_share & ~size_t(255), s);
+    if (st != TRIDI_SUCCESS) break;
+    if ((e = cudaMemcpyAsync(x + off, dx + off, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
+      st = cuda_status(e);
+      break;
+    }
+  }
+  cudaError_t e0 = cudaStreamSynchronize(w.stream[0]);
+  cudaError_t e1 = cudaStreamSynchronize(w.stream[1]);
+  if (st == TRIDI_SUCCESS && (e0 != cudaSuccess || e1 != cudaSuccess))
+    st = cuda_status(e0 != cudaSuccess ? e0 : e1);
+  return st;
+}
+
+const char* algo_name(int algo) {
+  static const char* names[] = {"cr", "pcr", "crpcr", "crNBC", "crpcrNBC", "crNBC", "pcrGauss"};
+  return algo >= 0 && algo < 7 ? names[algo] : "?";
+}
+
+// The C++ drop-ins: reference error behaviour (print, then exit like
+// CUDA_SAFE_CALL) and the optional reference timing line.
+template <class T>
+void dropin(int algo, T* a, T* b, T* c, T* d, T* x, int n, int m, int param) {
+  const char* timing = std::getenv("TRIDI_DROPIN_TIMING");
+  if (timing && timing[0] == '1') {
+    // numIterations (common.h:14) timed launches of the device work alone,
+    // printed like cr_app.cu:48: "<name>: numSystems: .., systemSize: .., GPU kernel time: .. ms".
+    host_solve<T>(algo, a, b, c, d, x, n, m, param);  // stage inputs + warm up
+    std::lock_guard<std::mutex> lock(g_mu);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    Workspace& w = g_ws[dev];
+    const size_t arr = align256((size_t)m * n * sizeof(T));
+    char* base = static_cast<char*>(w.ptr);
+    const size_t scratch = w.bytes - 5 * arr;
+    cudaStreamSynchronize(w.stream[0]);
+    auto t0 = std::chrono::steady_clock::now();
+    for (int i = 0; i < 50; ++i)
+      dropin_device_solve<T>(algo, reinterpret_cast<T*>(base), reinterpret_cast<T*>(base + arr),
+                             reinterpret_cast<T*>(base + 2 * arr), reinterpret_cast<T*>(base + 3 * arr),
+                             reinterpret_cast<T*>(base + 4 * arr), n, m, param, base + 5 * arr, scratch,
+                             w.stream[0]);
+    cudaStreamSynchronize(w.stream[0]);
+    double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (algo == TRIDI_DROPIN_PCR_THOMAS)
+      printf("pcrGauss: GPU kernel time: %f ms\n", ms / 50);
+    else
+      printf("%s: numSystems: %d, systemSize: %d, GPU kernel time: %f ms\n", algo_name(algo), m, n, ms / 50);
+  }
+  tridi_status st = host_solve<T>(algo, a, b, c, d, x, n, m, param);
+  if (st != TRIDI_SUCCESS) {
+    fprintf(stderr, "tridi: %s(systemSize=%d, numSystems=%d) failed: %s (cuda error %d)\n", algo_name(algo), n, m,
+            tridi_status_string(st), tridi_last_cuda_error());
+    const char* noexit = std::getenv("TRIDI_DROPIN_NO_EXIT");
+    if (!(noexit && noexit[0] == '1')) std::exit(1);
+  }
+}
+
+}  // namespace
+
+template <class T>
+size_t algo_scratch_bytes(int algo, int n, int m, int param);
+
+namespace {
+template <class T>
+size_t algo_scratch(int algo, int n, int m, int param) {
+  return algo_scratch_bytes<T>(algo, n, m, param);
+}
+}  // namespace
+
+}  // namespace tridi
+
+using tridi::dropin;
+
+void cr(float* a, float* b, float* c, float* d, float* x, int n, int m) { dropin<float>(TRIDI_DROPIN_CR, a, b, c, d, x, n, m, 0); }
+void cr(double* a, double* b, double* c, double* d, double* x, int n, int m) { dropin<double>(TRIDI_DROPIN_CR, a, b, c, d, x, n, m, 0); }
+void pcr(float* a, float* b, float* c, float* d, float* x, int n, int m) { dropin<float>(TRIDI_DROPIN_PCR, a, b, c, d, x, n, m, 0); }
+void pcr(double* a, double* b, double* c, double* d, double* x, int n, int m) { dropin<double>(TRIDI_DROPIN_PCR, a, b, c, d, x, n, m, 0); }
+void crpcr(float* a, float* b, float* c, float* d, float* x, int n, int m, int rest) { dropin<float>(TRIDI_DROPIN_CRPCR, a, b, c, d, x, n, m, rest); }
+void crpcr(double* a, double* b, double* c, double* d, double* x, int n, int m, int rest) { dropin<double>(TRIDI_DROPIN_CRPCR, a, b, c, d, x, n, m, rest); }
+void crNBC(float* a, float* b, float* c, float* d, float* x, int n, int m) { dropin<float>(TRIDI_DROPIN_CR_NBC, a, b, c, d, x, n, m, 0); }
+void crNBC(double* a, double* b, double* c, double* d, double* x, int n, int m) { dropin<double>(TRIDI_DROPIN_CR_NBC, a, b, c, d, x, n, m, 0); }
+void crpcrNBC(float* a, float* b, float* c, float* d, float* x, int n, int m, int rest) { dropin<float>(TRIDI_DROPIN_CRPCR_NBC, a, b, c, d, x, n, m, rest); }
+void crpcrNBC(double* a, double* b, double* c, double* d, double* x, int n, int m, int rest) { dropin<double>(TRIDI_DROPIN_CRPCR_NBC, a, b, c, d, x, n, m, rest); }
+void crNBC32(float* a, float* b, float* c, float* d, float* x, int n, int m) { dropin<float>(TRIDI_DROPIN_CR_NBC32, a, b, c, d, x, n, m, 0); }
+void crNBC32(double* a, double* b, double* c, double* d, double* x, int n, int m) { dropin<double>(TRIDI_DROPIN_CR_NBC32, a, b, c, d, x, n, m, 0); }
+void pcrGaussWrapper(float* a, float* b, float* c, float* d, float* x, int n, int m, int g) { dropin<float>(TRIDI_DROPIN_PCR_THOMAS, a, b, c, d, x, n, m, g); }
+void pcrGaussWrapper(double* a, double* b, double* c, double* d, double* x, int n, int m, int g) { dropin<double>(TRIDI_DROPIN_PCR_THOMAS, a, b, c, d, x, n, m, g); }
+
+extern "C" {
+
+tridi_status tridi_dropin_solve_f32(int algo, const float* a, const float* b, const float* c, const float* d,
+                                    float* x, int n, int m, int param) {
+  return tridi::host_solve<float>(algo, a, b, c, d, x, n, m, param);
+}
+tridi_status tridi_dropin_solve_f64(int algo, const double* a, const double* b, const double* c, const double* d,
+                                    double* x, int n, int m, int param) {
+  return tridi::host_solve<double>(algo, a, b, c, d, x, n, m, param);
+}
+tridi_status tridi_dropin_release(void) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return tridi::cuda_status(e);
+  std::lock_guard<std::mutex> lock(tridi::g_mu);
+  tridi::Workspace& w = tridi::g_ws[dev];
+  for (auto& s : w.stream)
+    if (s) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+      s = nullptr;
+    }
+  if (w.ptr) cudaFree(w.ptr);
+  w.ptr = nullptr;
+  w.bytes = 0;
+  return TRIDI_SUCCESS;
+}
+
+}  // extern "C"

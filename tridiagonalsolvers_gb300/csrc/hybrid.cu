@@ -1,0 +1,168 @@
+// Launch logic and C-ABI entry points of the CR / PCR / hybrid family
+// (hybrid.cuh).  Replaces the device work of cr() (cr_app.cu:4), pcr()
+// (pcr_app.cu:5) and crpcr() (crpcr_app.cu:5).
+#include "hybrid.cuh"
+#include "runtime.h"
+
+namespace tridi {
+
+namespace {
+
+// Per-(precision, n) shape: K rows per thread, TPS = n/K threads per system.
+// Groups of at most one warp use shuffles; wider groups use shared memory.
+struct Shape {
+  int K;
+  int tps;
+  bool warp;
+};
+
+template <class T>
+bool choose_shape(int n, Shape* s) {
+  if (!is_pow2(n) || n < 2) return false;
+  int K;
+  if (sizeof(T) == 4) {
+    if (n > 4096) return false;
+    K = n <= 16 ? n / 2 : (n == 512 || n == 4096 ? 16 : 8);
+  } else {
+    if (n > 2048) return false;
+    K = n <= 8 ? n / 2 : (n == 2048 ? 8 : 4);
+  }
+  s->K = K;
+  s->tps = n / K;
+  s->warp = s->tps <= 32;
+  return true;
+}
+
+constexpr int kWarpThreads = 128 + 32;   // 4 consumer warps + producer warp
+constexpr int kBlockThreads = 256 + 32;  // up to 8 consumer warps + producer
+
+template <class T, int K, bool WARP, int LSTRIDE>
+cudaError_t launch_one(const HybridParams& p0, const DeviceInfo& dev, cudaStream_t stream) {
+  constexpr int MAXT = WARP ? kWarpThreads : kBlockThreads;
+  constexpr int MINB = WARP ? 3 : 2;
+  auto kern = hybrid_kernel<T, K, WARP, LSTRIDE, MAXT, MINB>;
+  HybridParams p = p0;
+  const bool tma_ok = aligned16(p.a) && aligned16(p.b) && aligned16(p.c) && aligned16(p.d) && aligned16(p.x) &&
+                      ((size_t)p.n * sizeof(T)) % 16 == 0;
+  const int logk = Log2<K>::value;
+  const size_t stage_bytes = HybridSmem<T>::stage_elems(p.G, p.n) * sizeof(T);
+  const size_t fixed = HybridSmem<T>::bytes(0, p.G, p.n, p.scratch_rows, WARP, p.ct, logk);
+  int S = 0;
+  if (tma_ok) {
+    const size_t budget = 96 * 1024;
+    S = (int)(budget / stage_bytes);
+    if (S > 8) S = 8;
+    if (S < 1) S = 1;
+    while (S > 1 && fixed + S * stage_bytes > (size_t)dev.max_smem_optin) --S;
+    if (fixed + S * stage_bytes > (size_t)dev.max_smem_optin) S = 0;
+  }
+  p.stages = S;
+  const size_t smem = HybridSmem<T>::bytes(S, p.G, p.n, p.scratch_rows, WARP, p.ct, logk);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int threads = p.ct + 32;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  long grid = (long)per_sm * dev.sm_count;
+  if (grid > p.ntiles) grid = p.ntiles;
+  kern<<<(unsigned)grid, threads, smem, stream>>>(p);
+  return cudaGetLastError();
+}
+
+template <class T>
+tridi_status solve_hybrid(const T* a, const T* b, const T* c, const T* d, T* x, int n, int m, int stride,
+                          tridi_stream_t stream) {
+  if (!a || !b || !c || !d || !x || m <= 0) return TRIDI_ERROR_INVALID_VALUE;
+  Shape sh;
+  if (!choose_shape<T>(n, &sh)) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  const DeviceInfo* dev = current_device();
+  if (!dev) return TRIDI_ERROR_CUDA;
+  HybridParams p{};
+  p.a = a; p.b = b; p.c = c; p.d = d; p.x = x;
+  p.n = n; p.m = m; p.tps = sh.tps; p.stride = stride;
+  p.ct = sh.warp ? 128 : (sh.tps > 128 ? sh.tps : 128);
+  p.G = p.ct / sh.tps;
+  p.scratch_rows = stride < sh.K ? n / stride : sh.tps;
+  p.ntiles = (int)(((long)m + p.G - 1) / p.G);
+  p.status = dev->status;
+  cudaStream_t s = as_stream(stream);
+  cudaError_t e = cudaErrorInvalidValue;
+  const int ls = stride < sh.K ? stride : 0;
+#define TRIDI_LAUNCH_LS(KK, WW, LS) \
+  if (sh.K == KK && sh.warp == WW && ls == LS) e = launch_one<T, KK, WW, LS>(p, *dev, s);
+#define TRIDI_LAUNCH(KK, WW)                                                             \
+  TRIDI_LAUNCH_LS(KK, WW, 0)                                                              \
+  if constexpr (KK > 1) { TRIDI_LAUNCH_LS(KK, WW, 1) }                                    \
+  if constexpr (KK > 2) { TRIDI_LAUNCH_LS(KK, WW, (KK > 2 ? 2 : 1)) }                     \
+  if constexpr (KK > 4) { TRIDI_LAUNCH_LS(KK, WW, (KK > 4 ? 4 : 1)) }                     \
+  if constexpr (KK > 8) { TRIDI_LAUNCH_LS(KK, WW, (KK > 8 ? 8 : 1)) }
+  if constexpr (sizeof(T) == 4) {
+    TRIDI_LAUNCH(1, true) TRIDI_LAUNCH(2, true) TRIDI_LAUNCH(4, true) TRIDI_LAUNCH(8, true)
+    TRIDI_LAUNCH(16, true) TRIDI_LAUNCH(8, false) TRIDI_LAUNCH(16, false)
+  } else {
+    TRIDI_LAUNCH(1, true) TRIDI_LAUNCH(2, true) TRIDI_LAUNCH(4, true) TRIDI_LAUNCH(4, false)
+    TRIDI_LAUNCH(8, false)
+  }
+#undef TRIDI_LAUNCH
+#undef TRIDI_LAUNCH_LS
+  return cuda_status(e);
+}
+
+}  // namespace
+
+// Exposed to the other translation units (refinement, drop-ins).
+template <class T>
+tridi_status hybrid_solve_device(const T* a, const T* b, const T* c, const T* d, T* x, int n, int m, int stride,
+                                 tridi_stream_t stream) {
+  return solve_hybrid<T>(a, b, c, d, x, n, m, stride, stream);
+}
+template tridi_status hybrid_solve_device<float>(const float*, const float*, const float*, const float*, float*,
+                                                 int, int, int, tridi_stream_t);
+template tridi_status hybrid_solve_device<double>(const double*, const double*, const double*, const double*,
+                                                  double*, int, int, int, tridi_stream_t);
+
+}  // namespace tridi
+
+using tridi::solve_hybrid;
+
+namespace {
+template <class T>
+tridi_status crpcr_checked(const T* a, const T* b, const T* c, const T* d, T* x, int n, int m, int rest,
+                           tridi_stream_t s) {
+  if (n < 4 || !tridi::is_pow2(rest) || rest < 2 || rest > n / 2 || !tridi::is_pow2(n))
+    return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  return solve_hybrid<T>(a, b, c, d, x, n, m, n / rest, s);
+}
+}  // namespace
+
+extern "C" {
+
+tridi_status tridi_cr_f32(const float* a, const float* b, const float* c, const float* d, float* x, int n, int m,
+                          tridi_stream_t s) {
+  return solve_hybrid<float>(a, b, c, d, x, n, m, n / 2 > 0 ? n / 2 : 1, s);
+}
+tridi_status tridi_cr_f64(const double* a, const double* b, const double* c, const double* d, double* x, int n,
+                          int m, tridi_stream_t s) {
+  return solve_hybrid<double>(a, b, c, d, x, n, m, n / 2 > 0 ? n / 2 : 1, s);
+}
+tridi_status tridi_pcr_f32(const float* a, const float* b, const float* c, const float* d, float* x, int n, int m,
+                           tridi_stream_t s) {
+  if (n > 4096) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  return solve_hybrid<float>(a, b, c, d, x, n, m, 1, s);
+}
+tridi_status tridi_pcr_f64(const double* a, const double* b, const double* c, const double* d, double* x, int n,
+                           int m, tridi_stream_t s) {
+  return solve_hybrid<double>(a, b, c, d, x, n, m, 1, s);
+}
+tridi_status tridi_crpcr_f32(const float* a, const float* b, const float* c, const float* d, float* x, int n,
+                             int m, int rest, tridi_stream_t s) {
+  return crpcr_checked<float>(a, b, c, d, x, n, m, rest, s);
+}
+tridi_status tridi_crpcr_f64(const double* a, const double* b, const double* c, const double* d, double* x,
+                             int n, int m, int rest, tridi_stream_t s) {
+  return crpcr_checked<double>(a, b, c, d, x, n, m, rest, s);
+}
+
+}  // extern "C"

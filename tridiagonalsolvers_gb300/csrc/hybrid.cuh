@@ -1,0 +1,468 @@
+// The cyclic-reduction family on sm_103a: CR, PCR and the hybrid CR -> PCR ->
+// CR with a tunable switch level, all as one kernel template.
+//
+// Algorithm (the reference's, unchanged in its arithmetic):
+//   * CR forward levels s = 2, 4, ..., stride eliminate every row i with
+//     i % s == s-1 against rows i -/+ s/2 (right neighbour clamped to n-1),
+//     crpcr_kernel.cu:40-59.
+//   * The remaining rest = n/stride rows (i % stride == stride-1) form the
+//     intermediate system.  log2(rest/2) PCR steps with delta = 1, 2, ...,
+//     rest/4 (neighbours clamped to the first/last row) leave rest/2
+//     independent 2x2 systems (j, j + rest/2), crpcr_kernel.cu:81-119.
+//   * CR back substitution for levels s = stride, ..., 2, crpcr_kernel.cu:127-141.
+//   stride = n/2 is plain CR (cr_kernel.cu), stride = 1 is plain PCR
+//   (pcr_kernel.cu), anything between is crpcr with rest = n/stride.
+//
+// Mapping to the GB300 (not the reference's one-thread-per-pair layout):
+//   * A system is owned by a group of TPS = n/K threads; thread t holds rows
+//     [tK, tK+K) in registers.  The first log2(K) CR levels run inside each
+//     thread; only the thread's last row needs data from the next thread
+//     (one shuffle per level).
+//   * The cross-thread levels, the PCR steps and the 2x2 solves run on warp
+//     shuffles when the group fits in a warp (TPS <= 32) and on shared memory
+//     with named barriers otherwise.
+//   * Input rows arrive through a persistent pipeline: one producer warp
+//     streams whole tiles (G consecutive systems of a, b, c, d) into an
+//     S-stage shared-memory ring with cp.async.bulk + mbarrier transaction
+//     counts; the consumer warps read their rows with 16-byte shared loads,
+//     release the stage, solve, and write x with 16-byte global stores.
+//     Inputs too small or misaligned for bulk copies are read directly.
+#pragma once
+#include "tridi_device.cuh"
+
+namespace tridi {
+
+struct HybridParams {
+  const void* a;
+  const void* b;
+  const void* c;
+  const void* d;
+  void* x;
+  int n;         // system size (power of two)
+  int m;         // number of systems
+  int tps;       // threads per system, n / K
+  int G;         // systems per tile
+  int ntiles;    // ceil(m / G)
+  int stride;    // n / rest: 1 = PCR, n/2 = CR
+  int stages;    // pipeline depth (0 = direct loads, no bulk copies)
+  int ct;        // consumer threads per CTA = G * tps
+  int scratch_rows;  // rows of the block-path scratch per group
+  unsigned* status;
+};
+
+template <int V>
+struct Log2 {
+  static constexpr int value = 1 + Log2<V / 2>::value;
+};
+template <>
+struct Log2<1> {
+  static constexpr int value = 0;
+};
+
+// Shared-memory scratch used by the block (TPS > 32) path; laid out after the
+// pipeline stages.  Per group: 4 arrays of `rows` entries plus x.
+template <class T>
+struct GroupScratch {
+  T* a;
+  T* b;
+  T* c;
+  T* d;
+  T* x;
+  __device__ Row<T> get(int i) const { return {a[i], b[i], c[i], d[i]}; }
+  __device__ void put(int i, const Row<T>& r) const {
+    a[i] = r.a; b[i] = r.b; c[i] = r.c; d[i] = r.d;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// In-thread CR levels s = 2 .. SMAX (SMAX <= K), every row but the thread's
+// last (whose right neighbour lives in the next thread).
+template <class T, int K, int SMAX>
+__device__ __forceinline__ void local_forward(Row<T> (&r)[K]) {
+  constexpr int LOGK = Log2<K>::value;
+#pragma unroll
+  for (int j = 0; j < LOGK; ++j) {
+    const int s = 2 << j;
+    if (s <= SMAX) {
+#pragma unroll
+      for (int i = s - 1; i < K - 1; i += s) r[i] = reduce_row(r[i], r[i - s / 2], r[i + s / 2]);
+    }
+  }
+}
+
+// In-thread CR back substitution for levels s = SMAX .. 2.
+// xr[i] must already hold x for every row with i % (2*smax) == 2*smax-1
+// handled by coarser levels; x_prev is x of the previous thread's last row.
+template <class T, int K, int SMAX>
+__device__ __forceinline__ void local_backward(const Row<T> (&r)[K], T (&xr)[K], T x_prev, bool first_thread) {
+  constexpr int LOGK = Log2<K>::value;
+#pragma unroll
+  for (int j = LOGK - 1; j >= 0; --j) {
+    const int s = 2 << j;
+    if (s <= SMAX) {
+#pragma unroll
+      for (int i = s / 2 - 1; i < K; i += s) {
+        const bool edge = (i == s / 2 - 1);
+        const T xl = edge ? x_prev : xr[i >= s / 2 ? i - s / 2 : 0];
+        xr[i] = back_row(r[i], xl, xr[i + s / 2], edge && first_thread);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// PCR on the intermediate system when it has R = K/STRIDE rows per thread
+// (local rows STRIDE*q + STRIDE-1), warp-shuffle version (TPS <= 32).
+// Leaves x of those rows in xr.
+template <class T, int K, int STRIDE>
+__device__ __forceinline__ void pcr_regs_warp(const Row<T> (&r)[K], T (&xr)[K], int t, int tps) {
+  constexpr int R = K / STRIDE;
+  constexpr int LOGMAX = Log2<R>::value + 5;  // rest <= 32 * R
+  Row<T> y[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) y[q] = r[STRIDE * q + STRIDE - 1];
+  const int rest = tps * R;
+#pragma unroll
+  for (int e = 0; e < LOGMAX; ++e) {
+    const int dl = 1 << e;
+    if (4 * dl <= rest) {  // delta = 1 .. rest/4
+      const Row<T> first = shfl_idx(y[0], 0, tps);
+      const Row<T> last = shfl_idx(y[R - 1], tps - 1, tps);
+      Row<T> ny[R];
+      if (dl < R) {
+        Row<T> fromL[R], fromR[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+          if (q < dl) fromL[q] = shfl_up(y[(R - dl + q) % R], 1, tps);
+          if (q < dl) fromR[q] = shfl_down(y[q % R], 1, tps);
+        }
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+          Row<T> L, Rr;
+          if (q >= dl) L = y[(q - dl + R) % R];
+          else L = (t == 0) ? first : fromL[q];
+          if (q + dl < R) Rr = y[(q + dl) % R];
+          else Rr = (t == tps - 1) ? last : fromR[(q + dl - R + R) % R];
+          ny[q] = reduce_row(y[q], L, Rr);
+        }
+      } else {
+        const int ex = dl / R;  // whole threads away
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+          Row<T> L = shfl_up(y[q], ex, tps);
+          Row<T> Rr = shfl_down(y[q], ex, tps);
+          if (t < ex) L = first;
+          if (t + ex > tps - 1) Rr = last;
+          ny[q] = reduce_row(y[q], L, Rr);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < R; ++q) y[q] = ny[q];
+    }
+  }
+  // 2x2 systems (j, j + rest/2): same local slot, thread t ^ tps/2.
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const Row<T> p = shfl_xor(y[q], tps / 2, tps);
+    xr[STRIDE * q + STRIDE - 1] = (t < tps / 2) ? solve2_upper(y[q], p) : solve2_lower(p, y[q]);
+  }
+}
+
+// Same, shared-memory version for groups wider than a warp.
+template <class T, int K, int STRIDE>
+__device__ __forceinline__ void pcr_regs_block(const Row<T> (&r)[K], T (&xr)[K], int t, int tps,
+                                               const GroupScratch<T>& sc, int ct) {
+  constexpr int R = K / STRIDE;
+  Row<T> y[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    y[q] = r[STRIDE * q + STRIDE - 1];
+    sc.put(t * R + q, y[q]);
+  }
+  const int rest = tps * R;
+  consumer_sync(ct);
+  for (int dl = 1; 4 * dl <= rest; dl *= 2) {
+    Row<T> ny[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int j = t * R + q;
+      const int jl = j - dl < 0 ? 0 : j - dl;
+      const int jr = j + dl > rest - 1 ? rest - 1 : j + dl;
+      ny[q] = reduce_row(y[q], sc.get(jl), sc.get(jr));
+    }
+    consumer_sync(ct);
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      y[q] = ny[q];
+      sc.put(t * R + q, y[q]);
+    }
+    consumer_sync(ct);
+  }
+  const int half = rest / 2;
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int j = t * R + q;
+    xr[STRIDE * q + STRIDE - 1] = (j < half) ? solve2_upper(y[q], sc.get(j + half)) : solve2_lower(sc.get(j - half), y[q]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Whole-system solve for one group.  r: the thread's K rows (consumed), xr:
+// the thread's K unknowns (out).  LSTRIDE = 0 when the intermediate system
+// has at most one row per thread (stride >= K), else LSTRIDE = stride < K.
+template <class T, int K, bool WARP, int LSTRIDE>
+__device__ __forceinline__ void hybrid_solve(Row<T> (&r)[K], T (&xr)[K], int t, int tps, int stride,
+                                             const GroupScratch<T>& sc, Row<T>* exports, int ct) {
+  constexpr int LOGK = Log2<K>::value;
+  constexpr int SMAX = LSTRIDE == 0 ? K : LSTRIDE;  // last in-thread CR level
+  const bool last_thread = (t == tps - 1);
+  const int lane = threadIdx.x & 31;
+
+  // 1. In-thread CR levels for every row but the last.
+  local_forward<T, K, SMAX>(r);
+
+  // 2. The last row's CR levels: its right neighbour at level s is the next
+  //    thread's row s/2-1, already final after step 1.
+  if constexpr (!WARP) {
+    if (LOGK > 0 && lane == 0) {
+#pragma unroll
+      for (int j = 0; j < LOGK; ++j) exports[(threadIdx.x >> 5) * LOGK + j] = r[(1 << j) - 1];
+    }
+    consumer_sync(ct);
+  }
+#pragma unroll
+  for (int j = 0; j < LOGK; ++j) {
+    const int s = 2 << j;
+    if (s <= SMAX) {
+      Row<T> R = shfl_down(r[(1 << j) - 1], 1, WARP ? tps : 32);
+      if constexpr (!WARP) {
+        if (lane == 31 && !last_thread) R = exports[((threadIdx.x >> 5) + 1) * LOGK + j];
+      }
+      if (last_thread) R = r[K - 1];
+      r[K - 1] = reduce_row(r[K - 1], r[K - 1 - s / 2], R);
+    }
+  }
+
+  T x_prev;
+  if constexpr (LSTRIDE == 0) {
+    // 3a. One row per thread remains (row tK+K-1).  Cross-thread CR levels
+    //     until the intermediate system is reached (threads spaced P apart),
+    //     then PCR on it and the 2x2 solves, then CR back substitution.
+    Row<T> C = r[K - 1];
+    const int P = stride / K;
+    const int rest = tps / P;
+    const bool on = ((t + 1) & (P - 1)) == 0;
+    const int j = (t + 1) / P - 1;
+    T xC = T(0);
+    if constexpr (WARP) {
+      for (int D = 1; D < P; D *= 2) {
+        const Row<T> L = shfl_up(C, D, tps);
+        Row<T> R = shfl_down(C, D, tps);
+        if (last_thread) R = C;
+        if (((t + 1) & (2 * D - 1)) == 0) C = reduce_row(C, L, R);
+      }
+      for (int dl = 1; 4 * dl <= rest; dl *= 2) {
+        const int dd = dl * P;
+        Row<T> L = shfl_up(C, dd, tps);
+        Row<T> R = shfl_down(C, dd, tps);
+        const Row<T> F = shfl_idx(C, P - 1, tps);
+        const Row<T> Ls = shfl_idx(C, tps - 1, tps);
+        if (j - dl < 0) L = F;
+        if (j + dl > rest - 1) R = Ls;
+        if (on) C = reduce_row(C, L, R);
+      }
+      const Row<T> pr = shfl_xor(C, tps / 2, tps);
+      if (on) xC = (t < tps / 2) ? solve2_upper(C, pr) : solve2_lower(pr, C);
+      for (int D = P / 2; D >= 1; D /= 2) {
+        const T xl = __shfl_up_sync(kFull, xC, D, tps);
+        const T xrr = __shfl_down_sync(kFull, xC, D, tps);
+        if (((t + 1) & (2 * D - 1)) == D) xC = back_row(C, xl, xrr, t == D - 1);
+      }
+      x_prev = __shfl_up_sync(kFull, xC, 1, tps);
+    } else {
+      sc.put(t, C);
+      consumer_sync(ct);
+      for (int D = 1; D < P; D *= 2) {
+        if (((t + 1) & (2 * D - 1)) == 0) {
+          const int tr = t + D > tps - 1 ? tps - 1 : t + D;
+          C = reduce_row(C, sc.get(t - D), sc.get(tr));
+          sc.put(t, C);
+        }
+        consumer_sync(ct);
+      }
+      for (int dl = 1; 4 * dl <= rest; dl *= 2) {
+        Row<T> nc = C;
+        if (on) {
+          const int jl = j - dl < 0 ? 0 : j - dl;
+          const int jr = j + dl > rest - 1 ? rest - 1 : j + dl;
+          nc = reduce_row(C, sc.get((jl + 1) * P - 1), sc.get((jr + 1) * P - 1));
+        }
+        consumer_sync(ct);
+        if (on) {
+          C = nc;
+          sc.put(t, C);
+        }
+        consumer_sync(ct);
+      }
+      if (on) {
+        const int pt = t ^ (tps / 2);
+        xC = (t < tps / 2) ? solve2_upper(C, sc.get(pt)) : solve2_lower(sc.get(pt), C);
+        sc.x[t] = xC;
+      }
+      consumer_sync(ct);
+      for (int D = P / 2; D >= 1; D /= 2) {
+        if (((t + 1) & (2 * D - 1)) == D) {
+          const T xl = (t - D >= 0) ? sc.x[t - D] : T(0);
+          xC = back_row(C, xl, sc.x[t + D], t == D - 1);
+          sc.x[t] = xC;
+        }
+        consumer_sync(ct);
+      }
+      x_prev = (t > 0) ? sc.x[t - 1] : T(0);
+    }
+    xr[K - 1] = xC;
+  } else {
+    // 3b. The intermediate system has K/stride rows in every thread: PCR.
+    if constexpr (WARP) pcr_regs_warp<T, K, LSTRIDE>(r, xr, t, tps);
+    else pcr_regs_block<T, K, LSTRIDE>(r, xr, t, tps, sc, ct);
+    if constexpr (WARP) {
+      x_prev = __shfl_up_sync(kFull, xr[K - 1], 1, tps);
+    } else {
+      consumer_sync(ct);  // sc reused for x below
+      sc.x[t] = xr[K - 1];
+      consumer_sync(ct);
+      x_prev = (t > 0) ? sc.x[t - 1] : T(0);
+    }
+  }
+
+  // 4. In-thread CR back substitution.
+  local_backward<T, K, SMAX>(r, xr, x_prev, t == 0);
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory layout helpers (host and device agree on these).
+template <class T>
+struct HybridSmem {
+  // [full[S] | empty[S]] barriers (128 B), S stages of 4*G*n T, then the
+  // block-path scratch: G groups * 5 * rows T, then exports.
+  static __host__ __device__ size_t barrier_bytes() { return 128; }
+  static __host__ __device__ size_t stage_elems(int G, int n) { return (size_t)4 * G * n; }
+  static __host__ __device__ size_t bytes(int stages, int G, int n, int rows, bool warp, int ct, int logk) {
+    size_t s = barrier_bytes() + (size_t)stages * stage_elems(G, n) * sizeof(T);
+    if (!warp) {
+      s += (size_t)G * 5 * rows * sizeof(T);
+      s += (size_t)(ct / 32 + 1) * (logk > 0 ? logk : 1) * sizeof(Row<T>);
+    }
+    return s;
+  }
+};
+
+template <class T, int K, bool WARP, int LSTRIDE, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) hybrid_kernel(HybridParams p) {
+  constexpr int LOGK = Log2<K>::value;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* empty = full + 8;
+  const int S = p.stages;
+  const int n = p.n, G = p.G, tps = p.tps, ct = p.ct;
+  T* stages = reinterpret_cast<T*>(smem + HybridSmem<T>::barrier_bytes());
+  const size_t stage_elems = HybridSmem<T>::stage_elems(G, n);
+
+  const int tid = threadIdx.x;
+  const bool producer = tid >= ct;
+
+  if (tid == 0 && S > 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], ct / 32);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  const T* ga = static_cast<const T*>(p.a);
+  const T* gb = static_cast<const T*>(p.b);
+  const T* gc = static_cast<const T*>(p.c);
+  const T* gd = static_cast<const T*>(p.d);
+  T* gx = static_cast<T*>(p.x);
+
+  if (producer) {
+    // ---- producer warp: lane 0 streams tiles into the ring ----
+    if (S > 0 && (tid & 31) == 0) {
+      int k = 0;
+      for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++k) {
+        const int s = k % S;
+        if (k >= S && !mbar_wait(&empty[s], ((k / S) - 1) & 1, p.status)) break;
+        const long sys0 = (long)tile * G;
+        const long nsys = (p.m - sys0) < G ? (p.m - sys0) : G;
+        const uint32_t bytes = (uint32_t)(nsys * n * sizeof(T));
+        T* st = stages + s * stage_elems;
+        mbar_arrive_expect_tx(&full[s], 4 * bytes);
+        bulk_g2s(st + 0 * (size_t)G * n, ga + sys0 * n, bytes, &full[s]);
+        bulk_g2s(st + 1 * (size_t)G * n, gb + sys0 * n, bytes, &full[s]);
+        bulk_g2s(st + 2 * (size_t)G * n, gc + sys0 * n, bytes, &full[s]);
+        bulk_g2s(st + 3 * (size_t)G * n, gd + sys0 * n, bytes, &full[s]);
+      }
+    }
+    return;
+  }
+
+  // ---- consumer warps ----
+  const int g = tid / tps;
+  const int t = tid - g * tps;
+  GroupScratch<T> sc{};
+  Row<T>* exports = nullptr;
+  if constexpr (!WARP) {
+    T* base = stages + (size_t)S * stage_elems;
+    const size_t rows = p.scratch_rows;
+    T* mine = base + (size_t)g * 5 * rows;
+    sc = GroupScratch<T>{mine, mine + rows, mine + 2 * rows, mine + 3 * rows, mine + 4 * rows};
+    exports = reinterpret_cast<Row<T>*>(base + (size_t)G * 5 * rows);
+  }
+
+  int k = 0;
+  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++k) {
+    const long sys = (long)tile * G + g;
+    Row<T> r[K];
+    T va[K], vb[K], vc[K], vd[K];
+    bool ok = true;
+    if (S > 0) {
+      const int s = k % S;
+      ok = mbar_wait(&full[s], (k / S) & 1, p.status);
+      if constexpr (!WARP) ok = consumer_sync_and(ct, ok);
+      if (!ok) break;
+      const T* st = stages + s * stage_elems + (size_t)g * n + (size_t)t * K;
+      load_vec<T, K>(st + 0 * (size_t)G * n, va);
+      load_vec<T, K>(st + 1 * (size_t)G * n, vb);
+      load_vec<T, K>(st + 2 * (size_t)G * n, vc);
+      load_vec<T, K>(st + 3 * (size_t)G * n, vd);
+      __syncwarp();
+      if ((tid & 31) == 0) mbar_arrive(&empty[s]);
+    } else {
+      const long base = sys * n + (long)t * K;
+#pragma unroll
+      for (int i = 0; i < K; ++i) {
+        const bool in = sys < p.m;
+        va[i] = in ? ga[base + i] : T(0);
+        vb[i] = in ? gb[base + i] : T(1);
+        vc[i] = in ? gc[base + i] : T(0);
+        vd[i] = in ? gd[base + i] : T(0);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < K; ++i) r[i] = Row<T>{va[i], vb[i], vc[i], vd[i]};
+    T xr[K];
+    hybrid_solve<T, K, WARP, LSTRIDE>(r, xr, t, tps, p.stride, sc, exports, ct);
+    if (sys < p.m) {
+      T* dst = gx + sys * n + (long)t * K;
+      if (S > 0) store_vec<T, K>(dst, xr);
+      else {
+#pragma unroll
+        for (int i = 0; i < K; ++i) dst[i] = xr[i];
+      }
+    }
+  }
+  (void)LOGK;
+}
+
+}  // namespace tridi

@@ -1,0 +1,89 @@
+#include <mutex>
+
+#include "runtime.h"
+
+namespace tridi {
+
+namespace {
+constexpr int kMaxDevices = 64;
+DeviceInfo g_dev[kMaxDevices];
+std::mutex g_mu;
+thread_local int t_last_cuda_error = 0;
+}  // namespace
+
+tridi_status cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return TRIDI_SUCCESS;
+  t_last_cuda_error = static_cast<int>(e);
+  return TRIDI_ERROR_CUDA;
+}
+
+const DeviceInfo* current_device() {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cuda_status(e == cudaSuccess ? cudaErrorInvalidDevice : e);
+    return nullptr;
+  }
+  DeviceInfo& d = g_dev[dev];
+  if (d.status) return &d;
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (d.status) return &d;
+  int sms = 0, smem = 0;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) {
+    cuda_status(e);
+    return nullptr;
+  }
+  unsigned* st = nullptr;
+  if ((e = cudaMalloc(&st, 64)) != cudaSuccess || (e = cudaMemset(st, 0, 64)) != cudaSuccess) {
+    cuda_status(e);
+    return nullptr;
+  }
+  d.device = dev;
+  d.sm_count = sms;
+  d.max_smem_optin = smem;
+  d.status = st;
+  return &d;
+}
+
+}  // namespace tridi
+
+using namespace tridi;
+
+extern "C" {
+
+const char* tridi_version(void) { return "tridi-gb300 0.1 (sm_103a)"; }
+
+const char* tridi_status_string(tridi_status s) {
+  switch (s) {
+    case TRIDI_SUCCESS: return "success";
+    case TRIDI_ERROR_INVALID_VALUE: return "invalid value";
+    case TRIDI_ERROR_UNSUPPORTED_SIZE: return "unsupported system size";
+    case TRIDI_ERROR_MISALIGNED: return "pointer not 16-byte aligned";
+    case TRIDI_ERROR_CUDA: return "CUDA error";
+    case TRIDI_ERROR_DEVICE_TIMEOUT: return "bounded device wait timed out";
+    case TRIDI_ERROR_NOT_CONVERGED: return "iterative refinement did not converge";
+    case TRIDI_ERROR_OUT_OF_MEMORY: return "out of memory";
+    case TRIDI_ERROR_WORKSPACE_TOO_SMALL: return "workspace too small";
+    case TRIDI_ERROR_BUSY: return "queue full";
+  }
+  return "unknown status";
+}
+
+int tridi_last_cuda_error(void) { return t_last_cuda_error; }
+
+tridi_status tridi_init(void) { return current_device() ? TRIDI_SUCCESS : TRIDI_ERROR_CUDA; }
+
+tridi_status tridi_device_status(unsigned* bits, int reset) {
+  if (!bits) return TRIDI_ERROR_INVALID_VALUE;
+  const DeviceInfo* d = current_device();
+  if (!d) return TRIDI_ERROR_CUDA;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_status(e);
+  if ((e = cudaMemcpy(bits, d->status, sizeof(unsigned), cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return cuda_status(e);
+  if (reset && (e = cudaMemset(d->status, 0, sizeof(unsigned))) != cudaSuccess) return cuda_status(e);
+  return TRIDI_SUCCESS;
+}
+
+}  // extern "C"

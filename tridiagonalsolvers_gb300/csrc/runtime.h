@@ -1,0 +1,34 @@
+// Host-side runtime shared by every entry point: per-device facts (SM count,
+// shared-memory limit), the per-device status word that bounded device waits
+// report into, CUDA error capture, and the stream type conversion.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "tridi.h"
+
+namespace tridi {
+
+struct DeviceInfo {
+  int device = -1;
+  int sm_count = 0;
+  int max_smem_optin = 0;   // bytes of dynamic shared memory a CTA may opt into
+  unsigned* status = nullptr;  // device status word (TRIDI_DEVERR_* bits)
+};
+
+// Facts about the current device; allocates its status word on first use.
+// Returns nullptr and sets the thread's CUDA error if the device cannot be
+// queried.
+const DeviceInfo* current_device();
+
+// Records a CUDA error for tridi_last_cuda_error() and returns TRIDI_ERROR_CUDA
+// (or TRIDI_SUCCESS for cudaSuccess).
+tridi_status cuda_status(cudaError_t e);
+
+inline cudaStream_t as_stream(tridi_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+inline bool is_pow2(long v) { return v > 0 && (v & (v - 1)) == 0; }
+
+}  // namespace tridi

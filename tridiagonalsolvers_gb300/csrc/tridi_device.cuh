@@ -1,0 +1,199 @@
+// Device-side building blocks shared by every solver kernel: the row type,
+// the reduction formulas of the reference solvers, warp shuffles of rows,
+// and the sm_103a asynchronous-copy machinery (mbarrier + cp.async.bulk) with
+// bounded waits.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "tridi.h"
+
+namespace tridi {
+
+// One equation a*x[i-1] + b*x[i] + c*x[i+1] = d.
+template <class T>
+struct Row {
+  T a, b, c, d;
+};
+
+// Cyclic-reduction / PCR elimination of equation `me` against its two
+// neighbours L (at i - delta) and R (at i + delta).  This is the update of
+// the reference's solvers, written term for term in the same order so that
+// the rounding matches: cr_kernel.cu:53-58, pcr_kernel.cu:39-56,
+// crpcr_kernel.cu:50-55 and :92-98, crNBC.cu:68-73, pcrGauss_kernel.cu:89-98.
+template <class T>
+__device__ __forceinline__ Row<T> reduce_row(const Row<T>& me, const Row<T>& L, const Row<T>& R) {
+  T tmp1 = me.a / L.b;
+  T tmp2 = me.c / R.b;
+  Row<T> o;
+  o.b = me.b - L.c * tmp1 - R.a * tmp2;
+  o.d = me.d - L.d * tmp1 - R.d * tmp2;
+  o.a = -L.a * tmp1;
+  o.c = -R.c * tmp2;
+  return o;
+}
+
+// The 2x2 solve that closes CR / PCR (cr_kernel.cu:65-69, pcr_kernel.cu:67-71):
+// unknown 1 is the upper equation (r1), unknown 2 the lower (r2).
+template <class T>
+__device__ __forceinline__ T solve2_upper(const Row<T>& r1, const Row<T>& r2) {
+  T tmp3 = r2.b * r1.b - r1.c * r2.a;
+  return (r2.b * r1.d - r1.c * r2.d) / tmp3;
+}
+template <class T>
+__device__ __forceinline__ T solve2_lower(const Row<T>& r1, const Row<T>& r2) {
+  T tmp3 = r2.b * r1.b - r1.c * r2.a;
+  return (r2.d * r1.b - r1.d * r2.a) / tmp3;
+}
+
+// Back substitution of one unknown from its solved neighbours
+// (cr_kernel.cu:81-84).  `first` is the system's first row, which has no
+// left neighbour term.
+template <class T>
+__device__ __forceinline__ T back_row(const Row<T>& r, T xl, T xr, bool first) {
+  return first ? (r.d - r.c * xr) / r.b : (r.d - r.a * xl - r.c * xr) / r.b;
+}
+
+// ---- warp shuffles of rows -------------------------------------------------
+constexpr unsigned kFull = 0xffffffffu;
+
+template <class T>
+__device__ __forceinline__ Row<T> shfl_up(const Row<T>& v, int delta, int width) {
+  return {__shfl_up_sync(kFull, v.a, delta, width), __shfl_up_sync(kFull, v.b, delta, width),
+          __shfl_up_sync(kFull, v.c, delta, width), __shfl_up_sync(kFull, v.d, delta, width)};
+}
+template <class T>
+__device__ __forceinline__ Row<T> shfl_down(const Row<T>& v, int delta, int width) {
+  return {__shfl_down_sync(kFull, v.a, delta, width), __shfl_down_sync(kFull, v.b, delta, width),
+          __shfl_down_sync(kFull, v.c, delta, width), __shfl_down_sync(kFull, v.d, delta, width)};
+}
+template <class T>
+__device__ __forceinline__ Row<T> shfl_xor(const Row<T>& v, int mask, int width) {
+  return {__shfl_xor_sync(kFull, v.a, mask, width), __shfl_xor_sync(kFull, v.b, mask, width),
+          __shfl_xor_sync(kFull, v.c, mask, width), __shfl_xor_sync(kFull, v.d, mask, width)};
+}
+template <class T>
+__device__ __forceinline__ Row<T> shfl_idx(const Row<T>& v, int src, int width) {
+  return {__shfl_sync(kFull, v.a, src, width), __shfl_sync(kFull, v.b, src, width),
+          __shfl_sync(kFull, v.c, src, width), __shfl_sync(kFull, v.d, src, width)};
+}
+
+// ---- named barrier among the consumer warps (barrier 0 is __syncthreads) ---
+__device__ __forceinline__ void consumer_sync(int nthreads) {
+  asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
+// Barrier with an AND reduction of `pred` over the consumer threads.
+__device__ __forceinline__ bool consumer_sync_and(int nthreads, bool pred) {
+  uint32_t out;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 1, %2, p;\n selp.u32 %0, 1, 0, q;\n}"
+      : "=r"(out)
+      : "r"((uint32_t)pred), "r"(nthreads)
+      : "memory");
+  return out != 0;
+}
+
+// ---- mbarrier + bulk async copy (sm_90+ PTX, used here for sm_103a) --------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
+                   smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Upper bound on any wait in these kernels, in SM clock cycles (~1 s at the
+// GB300's 2 GHz maximum clock).  A wait that runs out records
+// TRIDI_DEVERR_WAIT_TIMEOUT in the status word and returns false; the caller
+// then stops issuing work and leaves the kernel.
+constexpr long long kWaitLimitCycles = 2000000000LL;
+
+__device__ __forceinline__ void record_error(unsigned* status, unsigned bit) {
+  if (status) atomicOr(status, bit);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* status) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > kWaitLimitCycles) {
+      record_error(status, TRIDI_DEVERR_WAIT_TIMEOUT);
+      return false;
+    }
+  }
+  return true;
+}
+
+// Bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned) from
+// global to this CTA's shared memory; completion is signalled on `bar` as
+// transaction bytes.
+__device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst_smem)),
+      "l"(src_gmem), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// ---- vector moves of K consecutive elements --------------------------------
+// Loads/stores K consecutive T from/to `p` (16-byte aligned when K*sizeof(T)
+// is a multiple of 16, which the callers guarantee) in 16-byte pieces.
+template <class T, int K>
+__device__ __forceinline__ void load_vec(const T* p, T (&v)[K]) {
+  if constexpr ((K * sizeof(T)) % 16 == 0) {
+    constexpr int PER = 16 / sizeof(T);
+#pragma unroll
+    for (int q = 0; q < K / PER; ++q) {
+      if constexpr (sizeof(T) == 4) {
+        float4 f = reinterpret_cast<const float4*>(p)[q];
+        v[q * 4 + 0] = f.x; v[q * 4 + 1] = f.y; v[q * 4 + 2] = f.z; v[q * 4 + 3] = f.w;
+      } else {
+        double2 f = reinterpret_cast<const double2*>(p)[q];
+        v[q * 2 + 0] = f.x; v[q * 2 + 1] = f.y;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < K; ++q) v[q] = p[q];
+  }
+}
+template <class T, int K>
+__device__ __forceinline__ void store_vec(T* p, const T (&v)[K]) {
+  if constexpr ((K * sizeof(T)) % 16 == 0) {
+    constexpr int PER = 16 / sizeof(T);
+#pragma unroll
+    for (int q = 0; q < K / PER; ++q) {
+      if constexpr (sizeof(T) == 4) {
+        reinterpret_cast<float4*>(p)[q] = make_float4(v[q * 4], v[q * 4 + 1], v[q * 4 + 2], v[q * 4 + 3]);
+      } else {
+        reinterpret_cast<double2*>(p)[q] = make_double2(v[q * 2], v[q * 2 + 1]);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < K; ++q) p[q] = v[q];
+  }
+}
+
+}  // namespace tridi
