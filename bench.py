@@ -299,7 +299,8 @@ def run_gpu(args):
     if rank == 0 and not args.no_table:
         cands = [("cr", lambda: lib.tridi_cr_f32(*ptrs, N, M, sp)),
                  ("crNBC", lambda: lib.tridi_cr_nbc_f32(*ptrs, N, M, sp)),
-                 ("pcr", lambda: lib.tridi_pcr_f32(*ptrs, N, M, sp))]
+                 ("pcr", lambda: lib.tridi_pcr_f32(*ptrs, N, M, sp)),
+                 ("partition", lambda: lib.tridi_solve_f32(*ptrs, N, M, sp))]
         rest = 2
         while rest <= N // 2:
             cands.append((f"crpcr_rest{rest}", (lambda r: lambda: lib.tridi_crpcr_f32(*ptrs, N, M, r, sp))(rest)))

@@ -61,6 +61,13 @@ tridi_status tridi_init(void);
    the current device since the last reset, and clears them when reset != 0. */
 tridi_status tridi_device_status(unsigned *bits, int reset);
 
+/* Launch-shape tunables (process-wide; 0 = automatic).  Used by the
+   autotuner and by experiments; they never change results, only speed. */
+#define TRIDI_TUNE_STAGES 1     /* cp.async.bulk pipeline stages per CTA (1..8) */
+#define TRIDI_TUNE_CRPCR_REST 2 /* switch level of the CR-PCR correction solves */
+tridi_status tridi_set_tunable(int key, int value);
+int tridi_get_tunable(int key);
+
 /* ---- the reference's solvers, device pointers ---------------------------- */
 /* Cyclic reduction.  Replaces cr() of cr_app.cu:4 / crKernel (cr_kernel.cu:1).
    n a power of two, 2 <= n <= 8192. */
@@ -99,6 +106,59 @@ tridi_status tridi_crpcr_nbc_f32(const float *a, const float *b, const float *c,
 tridi_status tridi_crpcr_nbc_f64(const double *a, const double *b, const double *c, const double *d,
                                  double *x, int n, int num_systems, int rest_system_size,
                                  tridi_stream_t stream);
+
+/* PCR-then-Thomas.  Replaces the device work of pcrGaussWrapper()
+   (pcrGauss_app.cu:164; kernels pcrKernelBranchFree + serial<T,g>,
+   pcrGauss_kernel.cu:1-126).  `gaussian` = g, the number of interleaved
+   subsystems (a power of two, 1 <= g <= n) solved by Thomas after log2(g) PCR
+   steps.  Exact for every g (the reference's step table is exact only when
+   g = 2^it).  Any 1 <= n <= 4096. */
+tridi_status tridi_pcr_thomas_f32(const float *a, const float *b, const float *c, const float *d, float *x, int n,
+                                  int num_systems, int gaussian, tridi_stream_t stream);
+tridi_status tridi_pcr_thomas_f64(const double *a, const double *b, const double *c, const double *d, double *x,
+                                  int n, int num_systems, int gaussian, tridi_stream_t stream);
+
+/* ---- GB300 additions (no counterpart kernel in the reference) ----------- */
+/* Generic batched solve, any size 1 <= n <= 8704 (FP64: <= 4608), not only
+   powers of two:
+   partition method (per-lane Thomas-like chunk elimination in registers,
+   PCR on the separator system, back substitution).  Uniform n, contiguous.
+   Checked against the gold Thomas solver of tridiagonal_gold.h:26-44. */
+tridi_status tridi_solve_f32(const float *a, const float *b, const float *c, const float *d, float *x, int n,
+                             int num_systems, tridi_stream_t stream);
+tridi_status tridi_solve_f64(const double *a, const double *b, const double *c, const double *d, double *x,
+                             int n, int num_systems, tridi_stream_t stream);
+
+/* Large systems, any n (up to 8704*16 unknowns in FP32, 4608*16 in FP64), in
+   either layout: TRIDI_LAYOUT_CONTIGUOUS (s*n + i) or TRIDI_LAYOUT_INTERLEAVED
+   (i*num_systems + s, system-fastest).  Three kernels on `stream`: chunk
+   elimination, separator-system solve, chunk back substitution.  Needs a
+   device workspace of tridi_large_workspace_bytes() bytes (no allocation
+   inside the call). */
+#define TRIDI_LAYOUT_CONTIGUOUS 0
+#define TRIDI_LAYOUT_INTERLEAVED 1
+size_t tridi_large_workspace_bytes(long n, long num_systems, int elem_size);
+tridi_status tridi_solve_large_f32(const float *a, const float *b, const float *c, const float *d, float *x, long n,
+                                   long num_systems, int layout, void *workspace, size_t workspace_bytes,
+                                   tridi_stream_t stream);
+tridi_status tridi_solve_large_f64(const double *a, const double *b, const double *c, const double *d, double *x,
+                                   long n, long num_systems, int layout, void *workspace, size_t workspace_bytes,
+                                   tridi_stream_t stream);
+
+/* Mixed-precision iterative refinement: FP32 a, b, c, d in, FP64 x out.
+   Only the residual r = d - T x and the accumulation x += e run in FP64;
+   every solve (the first and each correction) is an FP32 solve: CR-PCR for
+   power-of-two contiguous n <= 4096, the partition solver for other
+   contiguous n <= 8704, the large-system solver otherwise.  Stops when
+   max over systems of ||d - T x|| / ||d|| <= tol, or after max_sweeps
+   corrections (then returns TRIDI_ERROR_NOT_CONVERGED; x is still the best
+   iterate).  *sweeps receives the number of corrections applied and
+   *rel_residual the final maximum relative residual (either may be NULL).
+   Synchronises `stream` once per sweep to read the residual. */
+size_t tridi_refine_workspace_bytes(long n, long num_systems, int layout);
+tridi_status tridi_refine_f32(const float *a, const float *b, const float *c, const float *d, double *x, long n,
+                              long num_systems, int layout, double tol, int max_sweeps, void *workspace,
+                              size_t workspace_bytes, tridi_stream_t stream, int *sweeps, double *rel_residual);
 
 #ifdef __cplusplus
 }

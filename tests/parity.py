@@ -72,12 +72,14 @@ def check_ulps_where_reference_valid(x, x_ref, a, b, c, d, dtype=np.float32, ulp
     """check_ulps on the systems whose reference-kernel result itself passes the
     oracle's residual bound; returns (#systems compared, #reference failures).
 
-    The reference's cr / crNBC / crNBC32 kernels have no barrier between the
-    last forward level and the 2x2 solve (cr_kernel.cu:41-63, crNBC.cu:52-78):
-    thread 0 reads row n-1 that thread 1 wrote in that level.  Under
-    independent thread scheduling this is a race; on sm_103a it was observed
-    to corrupt FP64 results.  Systems where it struck are excluded here (the
-    product result is checked against the FP64 oracle regardless)."""
+    Where the reference kernel's own answer does not solve the system, the
+    comparison is meaningless; those systems are excluded here (the product
+    result is checked against the FP64 oracle regardless).  Observed on
+    sm_103a: the FP64 builds of crKernel and pcrKernel leave systems of 16
+    unknowns unsolved.  Both take their level count from
+    (int)log2(T(systemSize/2)) (cr_kernel.cu:11, pcr_kernel.cu:7).  By code
+    reading, cr / crNBC also lack a barrier between the last forward level and
+    the 2x2 solve (cr_kernel.cu:41-63, crNBC.cu:52-78)."""
     x_ref = np.asarray(x_ref)
     if dtype == np.float64:
         res, _ = _f64_metrics(a, b, c, d, x_ref, 0)

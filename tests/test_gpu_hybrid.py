@@ -138,7 +138,10 @@ def test_pcr_vs_reference_kernel(cuda, n, prec):
     a, b, c, d = workloads.dominant(64, n, seed=41 + n, dtype=dt)
     xr = _run_ref(rk, "pcr", cuda, a, b, c, d)
     x = _solve("pcr", cuda, a, b, c, d)
-    check_ulps(x, xr)
+    check_against_oracle(a, b, c, d, x, dtype=dt)
+    compared, ref_wrong = check_ulps_where_reference_valid(x, xr, a, b, c, d, dtype=dt)
+    if ref_wrong:
+        print(f"reference pcrKernel wrong on {ref_wrong}/{len(a)} systems (n={n}, {prec})")
 
 
 @pytest.mark.parametrize("n", [256, 1024])

@@ -1,0 +1,148 @@
+"""GPU parity of the bank-conflict-free shared-memory CR (crNBC / crNBC32 /
+crpcrNBC) and of the host-pointer drop-in launchers.  Tolerances:
+tests/parity.py."""
+import numpy as np
+import pytest
+
+import tridiagonalsolvers_gb300 as tg
+from oracle import gold
+from tridiagonalsolvers_gb300 import dropin, workloads
+
+from .parity import check_against_oracle, check_ulps, check_ulps_where_reference_valid, legacy_accept
+
+pytestmark = pytest.mark.gpu
+NP = {"f32": np.float32, "f64": np.float64}
+
+
+def _dev(cuda, *arrs):
+    import torch
+
+    return [torch.from_numpy(np.ascontiguousarray(v)).to(cuda) for v in arrs]
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("n", [2, 4, 8, 32, 64, 128, 256, 512, 1024, 2048])
+def test_cr_nbc_vs_oracle(cuda, n, prec):
+    import torch
+
+    dt = NP[prec]
+    for m in (1, 5, 77):
+        a, b, c, d = workloads.dominant(m, n, seed=300 + n + m, dtype=dt)
+        t = _dev(cuda, a, b, c, d)
+        x = tg.crNBC(*t).cpu().numpy()
+        x32 = tg.crNBC32(*t).cpu().numpy()
+        assert tg.device_status() == 0
+        check_against_oracle(a, b, c, d, x, dtype=dt)
+        assert np.array_equal(x, x32)
+        # the same CR arithmetic as the register kernel: agreement to a few ulp
+        xr = tg.cr(*t).cpu().numpy()
+        check_ulps(x, xr, ulps=4)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("n", [8, 64, 256, 1024])
+def test_crpcr_nbc_sweep(cuda, n, prec):
+    dt = NP[prec]
+    a, b, c, d = workloads.dominant(19, n, seed=17 + n, dtype=dt)
+    t = _dev(cuda, a, b, c, d)
+    rest = 2
+    while rest <= n // 2:
+        x = tg.crpcrNBC(*t, rest).cpu().numpy()
+        check_against_oracle(a, b, c, d, x, dtype=dt)
+        rest *= 2
+
+
+def test_nbc_misaligned_direct_path(cuda):
+    import torch
+
+    n, m = 128, 9
+    a, b, c, d = workloads.dominant(m, n, seed=8)
+    bufs = [torch.zeros(m * n + 1, dtype=torch.float32, device=cuda) for _ in range(5)]
+    views = [t_[1:] for t_ in bufs]
+    for v, h in zip(views[:4], (a, b, c, d)):
+        v.copy_(torch.from_numpy(h.ravel()))
+    tg.crNBC(*views[:4], x=views[4], system_size=n)
+    check_against_oracle(a, b, c, d, views[4].view(m, n).cpu().numpy())
+
+
+def _ref():
+    if not gold.RefKernels.available():
+        pytest.skip("reference kernels not built")
+    return gold.RefKernels()
+
+
+@pytest.mark.parametrize("kind", ["crNBC", "crNBC32"])
+@pytest.mark.parametrize("n", [16, 64, 256, 1024])
+def test_nbc_vs_reference_kernel(cuda, kind, n):
+    import torch
+
+    rk = _ref()
+    a, b, c, d = workloads.dominant(48, n, seed=61 + n)
+    t = _dev(cuda, a, b, c, d)
+    xr = torch.zeros_like(t[0])
+    rk.solve(kind, *t, xr, n, 48, 0, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    a2, b2, c2, d2 = _dev(cuda, a, b, c, d)
+    x = tg.crNBC(a2, b2, c2, d2).cpu().numpy()
+    check_ulps_where_reference_valid(x, xr.cpu().numpy(), a, b, c, d)
+
+
+@pytest.mark.parametrize("n", [64, 256])
+def test_crpcr_nbc_vs_reference_kernel(cuda, n):
+    import torch
+
+    rk = _ref()
+    a, b, c, d = workloads.dominant(24, n, seed=71 + n)
+    rest = 2
+    while rest <= n // 2:
+        t = _dev(cuda, a, b, c, d)
+        xr = torch.zeros_like(t[0])
+        rk.solve("crpcrNBC", *t, xr, n, 24, rest, torch.cuda.current_stream().cuda_stream)
+        x = tg.crpcrNBC(*_dev(cuda, a, b, c, d), rest).cpu().numpy()
+        check_ulps(x, xr.cpu().numpy())
+        rest *= 2
+
+
+# ---- host-pointer drop-ins ---------------------------------------------------
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("name", ["cr", "pcr", "crNBC", "crNBC32"])
+def test_dropin_matches_device_path(cuda, name, prec):
+    dt = NP[prec]
+    n, m = 256, 3000  # several chunks of whole systems
+    a, b, c, d = workloads.dominant(m, n, seed=5, dtype=dt)
+    keep = [v.copy() for v in (a, b, c, d)]
+    x = np.zeros_like(a)
+    getattr(dropin, name)(a, b, c, d, x, n, m)
+    for u, v in zip((a, b, c, d), keep):
+        assert np.array_equal(u, v)
+    dev_fn = {"cr": tg.cr, "pcr": tg.pcr, "crNBC": tg.crNBC, "crNBC32": tg.crNBC32}[name]
+    xd = dev_fn(*_dev(cuda, a, b, c, d)).cpu().numpy()
+    assert np.array_equal(x, xd)
+    check_against_oracle(a, b, c, d, x, dtype=dt)
+    if prec == "f32":
+        legacy_accept(x, a, b, c, d)
+
+
+@pytest.mark.parametrize("name", ["crpcr", "crpcrNBC"])
+def test_dropin_hybrids(cuda, name):
+    n, m = 512, 700
+    a, b, c, d = workloads.dominant(m, n, seed=6)
+    for rest in (2, 16, 256):
+        x = np.zeros_like(a)
+        getattr(dropin, name)(a, b, c, d, x, n, m, rest)
+        check_against_oracle(a, b, c, d, x)
+
+
+def test_dropin_large_batch_chunks(cuda):
+    n, m = 256, 65536
+    a, b, c, d = workloads.dominant(m, n, seed=workloads.SEEDS["c2"])
+    x = np.zeros_like(a)
+    dropin.cr(a, b, c, d, x, n, m)
+    sel = np.r_[0:32, 8190:8194, m - 32:m]
+    check_against_oracle(a[sel], b[sel], c[sel], d[sel], x[sel])
+
+
+def test_dropin_rejects_bad_sizes(cuda):
+    a = np.zeros((2, 300), np.float32)
+    with pytest.raises(tg.TridiError):
+        dropin.cr(a, a.copy(), a.copy(), a.copy(), a.copy(), 300, 2)

@@ -36,12 +36,24 @@ _SIGS: dict[str, tuple] = {
     "tridi_last_cuda_error": (c_int, []),
     "tridi_init": (c_int, []),
     "tridi_device_status": (c_int, [POINTER(c_uint), c_int]),
+    "tridi_set_tunable": (c_int, [c_int, c_int]),
+    "tridi_get_tunable": (c_int, [c_int]),
 }
 for _prec in ("f32", "f64"):
     for _name in ("cr", "pcr", "cr_nbc"):
         _SIGS[f"tridi_{_name}_{_prec}"] = (c_int, [_P, _P, _P, _P, _P, c_int, c_int, _P])
     for _name in ("crpcr", "crpcr_nbc"):
         _SIGS[f"tridi_{_name}_{_prec}"] = (c_int, [_P, _P, _P, _P, _P, c_int, c_int, c_int, _P])
+    _SIGS[f"tridi_solve_{_prec}"] = (c_int, [_P, _P, _P, _P, _P, c_int, c_int, _P])
+    _SIGS[f"tridi_pcr_thomas_{_prec}"] = (c_int, [_P, _P, _P, _P, _P, c_int, c_int, c_int, _P])
+    _SIGS[f"tridi_dropin_solve_{_prec}"] = (c_int, [c_int, _P, _P, _P, _P, _P, c_int, c_int, c_int])
+    _SIGS[f"tridi_solve_large_{_prec}"] = (c_int, [_P, _P, _P, _P, _P, ctypes.c_long, ctypes.c_long, c_int, _P,
+                                                   c_size_t, _P])
+_SIGS["tridi_dropin_release"] = (c_int, [])
+_SIGS["tridi_large_workspace_bytes"] = (c_size_t, [ctypes.c_long, ctypes.c_long, c_int])
+_SIGS["tridi_refine_workspace_bytes"] = (c_size_t, [ctypes.c_long, ctypes.c_long, c_int])
+_SIGS["tridi_refine_f32"] = (c_int, [_P, _P, _P, _P, _P, ctypes.c_long, ctypes.c_long, c_int, c_double, c_int, _P,
+                                     c_size_t, _P, POINTER(c_int), POINTER(c_double)])
 
 
 def declared_symbols() -> list[str]:

@@ -16,6 +16,8 @@ struct Abi<float> {
   static constexpr auto crpcr = tridi_crpcr_f32;
   static constexpr auto cr_nbc = tridi_cr_nbc_f32;
   static constexpr auto crpcr_nbc = tridi_crpcr_nbc_f32;
+  static constexpr auto pcr_thomas = tridi_pcr_thomas_f32;
+  static constexpr auto solve = tridi_solve_f32;
 };
 template <>
 struct Abi<double> {
@@ -24,6 +26,8 @@ struct Abi<double> {
   static constexpr auto crpcr = tridi_crpcr_f64;
   static constexpr auto cr_nbc = tridi_cr_nbc_f64;
   static constexpr auto crpcr_nbc = tridi_crpcr_nbc_f64;
+  static constexpr auto pcr_thomas = tridi_pcr_thomas_f64;
+  static constexpr auto solve = tridi_solve_f64;
 };
 }  // namespace
 
@@ -45,6 +49,12 @@ tridi_status dropin_device_solve(int algo, const T* a, const T* b, const T* c, c
     case TRIDI_DROPIN_CR_NBC:
     case TRIDI_DROPIN_CR_NBC32: return Abi<T>::cr_nbc(a, b, c, d, x, n, m, st);
     case TRIDI_DROPIN_CRPCR_NBC: return Abi<T>::crpcr_nbc(a, b, c, d, x, n, m, param, st);
+    case TRIDI_DROPIN_PCR_THOMAS:
+      // pcrGaussWrapper: PCR-then-Thomas up to 4096 unknowns; beyond, the
+      // exact partition solver (the reference switches to its global-memory
+      // PCR + chunked Thomas path above MINSYSTEM = 1024, pcrGauss_app.cu:196).
+      if (n <= 4096) return Abi<T>::pcr_thomas(a, b, c, d, x, n, m, param, st);
+      return Abi<T>::solve(a, b, c, d, x, n, m, st);
     default: return TRIDI_ERROR_INVALID_VALUE;
   }
 }

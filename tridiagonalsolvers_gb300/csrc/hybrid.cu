@@ -47,15 +47,7 @@ cudaError_t launch_one(const HybridParams& p0, const DeviceInfo& dev, cudaStream
   const int logk = Log2<K>::value;
   const size_t stage_bytes = HybridSmem<T>::stage_elems(p.G, p.n) * sizeof(T);
   const size_t fixed = HybridSmem<T>::bytes(0, p.G, p.n, p.scratch_rows, WARP, p.ct, logk);
-  int S = 0;
-  if (tma_ok) {
-    const size_t budget = 96 * 1024;
-    S = (int)(budget / stage_bytes);
-    if (S > 8) S = 8;
-    if (S < 1) S = 1;
-    while (S > 1 && fixed + S * stage_bytes > (size_t)dev.max_smem_optin) --S;
-    if (fixed + S * stage_bytes > (size_t)dev.max_smem_optin) S = 0;
-  }
+  const int S = tma_ok ? pick_stages(fixed, stage_bytes, 2, dev) : 0;
   p.stages = S;
   const size_t smem = HybridSmem<T>::bytes(S, p.G, p.n, p.scratch_rows, WARP, p.ct, logk);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -38,10 +38,7 @@ tridi_status solve_nbc(const T* a, const T* b, const T* c, const T* d, T* x, int
       continue;
     }
     if (fixed + 2 * stage <= target || (G == 1 && fixed + stage <= limit)) {
-      const size_t budget = fixed + 2 * stage <= target ? target : limit;
-      S = (int)((budget - fixed) / stage);
-      if (S > 8) S = 8;
-      if (S < 1) S = 1;
+      S = pick_stages(fixed, stage, 1, *dev);
       break;
     }
   }

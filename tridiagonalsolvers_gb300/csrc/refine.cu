@@ -1,0 +1,291 @@
+// Mixed-precision iterative refinement: FP32 solves, FP64 residual and FP64
+// accumulation of the corrections.  No counterpart in the reference (its
+// solvers are FP32 or FP64 throughout, common.h:8-12); the oracle is the gold
+// Thomas solver run in FP64 (tridiagonal_gold.h:26-44).
+//
+//   e0 = solve32(T, d)
+//   sweep k = 0, 1, ...:
+//     x_{k+1} = x_k + e_k                 (FP64; x_0 = 0)
+//     r = d - T x_{k+1}                   (FP64; stored as FP32 for the next solve)
+//     rel_s = ||r_s|| / ||d_s|| per system; stop when max_s rel_s <= tol
+//     e_{k+1} = solve32(T, r)             (the same FP32 kernels as a plain solve)
+// The update and the residual are one kernel (refine_update_residual); x is
+// ping-ponged between two FP64 buffers so neighbours are read before they
+// are rewritten.  Only those two steps touch FP64 arithmetic.
+#include <cmath>
+
+#include "runtime.h"
+#include "tridi_device.cuh"
+
+namespace tridi {
+
+template <class T>
+tridi_status hybrid_solve_device(const T*, const T*, const T*, const T*, T*, int, int, int, tridi_stream_t);
+template <class T>
+tridi_status partition_solve_device(const T*, const T*, const T*, const T*, T*, int, int, tridi_stream_t);
+template <class T>
+tridi_status large_solve_device(const T*, const T*, const T*, const T*, T*, long, long, int, void*, size_t,
+                                tridi_stream_t);
+
+struct RefineParams {
+  const float *a, *b, *c, *d;
+  const float* e;     // FP32 correction
+  const double* xin;  // x_k (ignored when first)
+  double* xout;       // x_{k+1}
+  float* r;           // FP32 copy of the residual
+  double* rr;         // per-system sum of r^2 (accumulated)
+  double* dd;         // per-system sum of d^2 (accumulated on the first sweep)
+  long n, m;
+  int layout;
+  int first;
+  int rows_per_block;  // contiguous: elements per block per system chunk; interleaved: rows per block
+};
+
+// x_{k+1} at (i, s) without writing it: x_k + e (or e on the first sweep).
+__device__ __forceinline__ double xnew(const RefineParams& p, long k) {
+  return p.first ? (double)p.e[k] : p.xin[k] + (double)p.e[k];
+}
+
+__device__ __forceinline__ double residual_at(const RefineParams& p, long i, long k, long stride, double xi,
+                                              double* dsq) {
+  const double di = (double)p.d[k];
+  double r = di - (double)p.b[k] * xi;
+  if (i > 0) r -= (double)p.a[k] * xnew(p, k - stride);
+  if (i < p.n - 1) r -= (double)p.c[k] * xnew(p, k + stride);
+  *dsq = di * di;
+  return r;
+}
+
+// Contiguous layout: block (system s, chunk q) covers rows [q*R, q*R + R).
+__global__ void __launch_bounds__(256) refine_contig_kernel(RefineParams p) {
+  const long chunks = (p.n + p.rows_per_block - 1) / p.rows_per_block;
+  const long s = blockIdx.x / chunks, q = blockIdx.x % chunks;
+  double rs = 0.0, ds = 0.0;
+  const long i0 = q * p.rows_per_block;
+  const long i1 = i0 + p.rows_per_block < p.n ? i0 + p.rows_per_block : p.n;
+  for (long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    const long k = s * p.n + i;
+    const double xi = xnew(p, k);
+    double dsq;
+    const double r = residual_at(p, i, k, 1, xi, &dsq);
+    p.xout[k] = xi;
+    p.r[k] = (float)r;
+    rs += r * r;
+    ds += dsq;
+  }
+  __shared__ double red[2][8];
+  for (int o = 16; o > 0; o >>= 1) {
+    rs += __shfl_down_sync(kFull, rs, o);
+    ds += __shfl_down_sync(kFull, ds, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = rs;
+    red[1][threadIdx.x >> 5] = ds;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a0 = 0, a1 = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a0 += red[0][w];
+      a1 += red[1][w];
+    }
+    atomicAdd(&p.rr[s], a0);
+    if (p.first) atomicAdd(&p.dd[s], a1);
+  }
+}
+
+// Interleaved layout: block = 32 systems x 8 row lanes, rows [q*R, q*R + R).
+__global__ void __launch_bounds__(256) refine_inter_kernel(RefineParams p) {
+  const long groups = (p.m + 31) / 32;
+  const long g = blockIdx.x % groups, q = blockIdx.x / groups;
+  const long s = g * 32 + (threadIdx.x & 31);
+  const int lr = threadIdx.x >> 5;
+  double rs = 0.0, ds = 0.0;
+  const long i0 = q * p.rows_per_block;
+  const long i1 = i0 + p.rows_per_block < p.n ? i0 + p.rows_per_block : p.n;
+  if (s < p.m) {
+    for (long i = i0 + lr; i < i1; i += 8) {
+      const long k = i * p.m + s;
+      const double xi = xnew(p, k);
+      double dsq;
+      const double r = residual_at(p, i, k, p.m, xi, &dsq);
+      p.xout[k] = xi;
+      p.r[k] = (float)r;
+      rs += r * r;
+      ds += dsq;
+    }
+  }
+  __shared__ double red[2][8][32];
+  red[0][lr][threadIdx.x & 31] = rs;
+  red[1][lr][threadIdx.x & 31] = ds;
+  __syncthreads();
+  if (lr == 0 && s < p.m) {
+    double a0 = 0, a1 = 0;
+    for (int w = 0; w < 8; ++w) {
+      a0 += red[0][w][threadIdx.x];
+      a1 += red[1][w][threadIdx.x];
+    }
+    atomicAdd(&p.rr[s], a0);
+    if (p.first) atomicAdd(&p.dd[s], a1);
+  }
+}
+
+// max over systems of sqrt(rr/dd) into out[0].
+__global__ void refine_maxrel_kernel(const double* rr, const double* dd, long m, double* out) {
+  double v = 0.0;
+  for (long s = threadIdx.x; s < m; s += blockDim.x) {
+    const double den = dd[s] > 0 ? dd[s] : 1.0;
+    const double q = sqrt(rr[s] / den);
+    v = q > v || q != q ? q : v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double w = __shfl_down_sync(kFull, v, o);
+    v = w > v || w != w ? w : v;
+  }
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double w = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) w = red[i] > w || red[i] != red[i] ? red[i] : w;
+    out[0] = w;
+  }
+}
+
+namespace {
+
+long align64(long v) { return (v + 63) & ~63L; }
+
+// Workspace layout (bytes): e (4 nm), r (4 nm), xalt (8 nm), rr (8 m), dd (8 m),
+// scalar (8), then the large solver's workspace if needed.
+struct RefineWs {
+  float* e;
+  float* r;
+  double* xalt;
+  double* rr;
+  double* dd;
+  double* scalar;
+  void* inner;
+  size_t inner_bytes;
+};
+
+bool needs_large(long n, long m, int layout) {
+  (void)m;
+  return layout == TRIDI_LAYOUT_INTERLEAVED || n > 8704;
+}
+
+size_t inner_bytes(long n, long m, int layout) {
+  return needs_large(n, m, layout) ? tridi_large_workspace_bytes(n, m, 4) : 0;
+}
+
+size_t refine_ws_bytes(long n, long m, int layout) {
+  const long nm = align64(n * m);
+  return (size_t)nm * (4 + 4 + 8) + (size_t)align64(m) * 16 + 256 + inner_bytes(n, m, layout) + 1024;
+}
+
+RefineWs carve(void* ws, long n, long m, int layout) {
+  char* w = static_cast<char*>(ws);
+  const long nm = align64(n * m);
+  RefineWs r;
+  r.e = reinterpret_cast<float*>(w); w += nm * 4;
+  r.r = reinterpret_cast<float*>(w); w += nm * 4;
+  r.xalt = reinterpret_cast<double*>(w); w += nm * 8;
+  r.rr = reinterpret_cast<double*>(w); w += align64(m) * 8;
+  r.dd = reinterpret_cast<double*>(w); w += align64(m) * 8;
+  r.scalar = reinterpret_cast<double*>(w); w += 256;
+  r.inner = w;
+  r.inner_bytes = inner_bytes(n, m, layout);
+  return r;
+}
+
+int default_rest(int n) {
+  const int t = tunable(TRIDI_TUNE_CRPCR_REST);
+  int rest = t > 0 ? t : 4;
+  while (rest > n / 2 && rest > 2) rest /= 2;
+  return rest;
+}
+
+// The FP32 solve used for the first solution and every correction.
+tridi_status solve32(const float* a, const float* b, const float* c, const float* rhs, float* out, long n, long m,
+                     int layout, const RefineWs& w, tridi_stream_t s) {
+  if (needs_large(n, m, layout)) return large_solve_device<float>(a, b, c, rhs, out, n, m, layout, w.inner,
+                                                                   w.inner_bytes, s);
+  if (is_pow2(n) && n >= 4 && n <= 4096)
+    return hybrid_solve_device<float>(a, b, c, rhs, out, (int)n, (int)m, (int)n / default_rest((int)n), s);
+  return partition_solve_device<float>(a, b, c, rhs, out, (int)n, (int)m, s);
+}
+
+}  // namespace
+
+tridi_status refine_device(const float* a, const float* b, const float* c, const float* d, double* x, long n, long m,
+                           int layout, double tol, int max_sweeps, void* ws, size_t ws_bytes, tridi_stream_t stream,
+                           int* sweeps_out, double* res_out) {
+  if (!a || !b || !c || !d || !x || n <= 0 || m <= 0 || max_sweeps < 0 || (layout != 0 && layout != 1))
+    return TRIDI_ERROR_INVALID_VALUE;
+  if (!ws || ws_bytes < refine_ws_bytes(n, m, layout)) return TRIDI_ERROR_WORKSPACE_TOO_SMALL;
+  if (!current_device()) return TRIDI_ERROR_CUDA;
+  const RefineWs w = carve(ws, n, m, layout);
+  cudaStream_t st = as_stream(stream);
+  cudaError_t e;
+  tridi_status ts = solve32(a, b, c, d, w.e, n, m, layout, w, stream);
+  if (ts != TRIDI_SUCCESS) return ts;
+  if ((e = cudaMemsetAsync(w.dd, 0, sizeof(double) * m, st)) != cudaSuccess) return cuda_status(e);
+
+  RefineParams p{};
+  p.a = a; p.b = b; p.c = c; p.d = d; p.e = w.e; p.r = w.r; p.rr = w.rr; p.dd = w.dd;
+  p.n = n; p.m = m; p.layout = layout;
+  double* bufs[2] = {x, w.xalt};
+  int cur = 0;  // x_k lives in bufs[cur]
+  double rel = 0.0;
+  int sweep = 0;
+  for (;; ++sweep) {
+    p.first = sweep == 0;
+    p.xin = bufs[cur];
+    p.xout = bufs[cur ^ 1];
+    if (sweep == 0) p.xout = x;  // the first update writes x directly
+    if ((e = cudaMemsetAsync(w.rr, 0, sizeof(double) * m, st)) != cudaSuccess) return cuda_status(e);
+    unsigned blocks;
+    if (layout == 0) {
+      p.rows_per_block = n < 2048 ? (int)n : 2048;
+      const long chunks = (n + p.rows_per_block - 1) / p.rows_per_block;
+      blocks = (unsigned)(m * chunks);
+      refine_contig_kernel<<<blocks, 256, 0, st>>>(p);
+    } else {
+      p.rows_per_block = 256;
+      const long groups = (m + 31) / 32, chunks = (n + 255) / 256;
+      blocks = (unsigned)(groups * chunks);
+      refine_inter_kernel<<<blocks, 256, 0, st>>>(p);
+    }
+    cur = (p.xout == x) ? 0 : 1;
+    refine_maxrel_kernel<<<1, 1024, 0, st>>>(w.rr, w.dd, m, w.scalar);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+    if ((e = cudaMemcpyAsync(&rel, w.scalar, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+      return cuda_status(e);
+    if (rel <= tol || sweep >= max_sweeps || !(rel == rel)) break;
+    ts = solve32(a, b, c, w.r, w.e, n, m, layout, w, stream);
+    if (ts != TRIDI_SUCCESS) return ts;
+  }
+  if (cur != 0 &&
+      (e = cudaMemcpyAsync(x, bufs[cur], sizeof(double) * n * m, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
+    return cuda_status(e);
+  if (sweeps_out) *sweeps_out = sweep;
+  if (res_out) *res_out = rel;
+  return rel <= tol ? TRIDI_SUCCESS : TRIDI_ERROR_NOT_CONVERGED;
+}
+
+}  // namespace tridi
+
+extern "C" {
+
+size_t tridi_refine_workspace_bytes(long n, long num_systems, int layout) {
+  return tridi::refine_ws_bytes(n, num_systems, layout);
+}
+
+tridi_status tridi_refine_f32(const float* a, const float* b, const float* c, const float* d, double* x, long n,
+                              long m, int layout, double tol, int max_sweeps, void* ws, size_t ws_bytes,
+                              tridi_stream_t s, int* sweeps, double* rel_residual) {
+  return tridi::refine_device(a, b, c, d, x, n, m, layout, tol, max_sweeps, ws, ws_bytes, s, sweeps, rel_residual);
+}
+
+}  // extern "C"

@@ -9,7 +9,20 @@ constexpr int kMaxDevices = 64;
 DeviceInfo g_dev[kMaxDevices];
 std::mutex g_mu;
 thread_local int t_last_cuda_error = 0;
+constexpr int kTunables = 8;
+int g_tunable[kTunables] = {};
 }  // namespace
+
+int tunable(int key) { return key >= 0 && key < kTunables ? g_tunable[key] : 0; }
+
+int pick_stages(size_t fixed_bytes, size_t stage_bytes, int fallback, const DeviceInfo& dev) {
+  int S = tunable(TRIDI_TUNE_STAGES);
+  if (S <= 0) S = fallback;
+  if (S > 8) S = 8;
+  while (S > 1 && fixed_bytes + S * stage_bytes > (size_t)dev.max_smem_optin) --S;
+  if (fixed_bytes + S * stage_bytes > (size_t)dev.max_smem_optin) S = 0;
+  return S;
+}
 
 tridi_status cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return TRIDI_SUCCESS;
@@ -71,6 +84,14 @@ const char* tridi_status_string(tridi_status s) {
 }
 
 int tridi_last_cuda_error(void) { return t_last_cuda_error; }
+
+tridi_status tridi_set_tunable(int key, int value) {
+  if (key < 0 || key >= kTunables || value < 0) return TRIDI_ERROR_INVALID_VALUE;
+  g_tunable[key] = value;
+  return TRIDI_SUCCESS;
+}
+
+int tridi_get_tunable(int key) { return tunable(key); }
 
 tridi_status tridi_init(void) { return current_device() ? TRIDI_SUCCESS : TRIDI_ERROR_CUDA; }
 

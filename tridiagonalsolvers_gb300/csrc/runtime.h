@@ -28,6 +28,13 @@ tridi_status cuda_status(cudaError_t e);
 
 inline cudaStream_t as_stream(tridi_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Launch-shape tunables (tridi_set_tunable); 0 means "choose automatically".
+int tunable(int key);
+
+// Pipeline depth for a tiled kernel: the tunable if set, else `fallback`,
+// reduced until the shared memory fits the device.
+int pick_stages(size_t fixed_bytes, size_t stage_bytes, int fallback, const DeviceInfo& dev);
+
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 inline bool is_pow2(long v) { return v > 0 && (v & (v - 1)) == 0; }
 

@@ -10,6 +10,15 @@
 
 namespace tridi {
 
+// Division used by every solver kernel.  FP32: __fdividef, the reciprocal
+// (MUFU) times the numerator: at most 2 ulp from the IEEE quotient, no
+// slow-path branch (divisors here are O(1), far from the 2^126 limit of the
+// intrinsic).  FP64: the IEEE quotient.  Each division of the reference's
+// formulas becomes one tdiv, so results stay within a few ulp of the
+// reference's arithmetic.
+__device__ __forceinline__ float tdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double tdiv(double a, double b) { return a / b; }
+
 // One equation a*x[i-1] + b*x[i] + c*x[i+1] = d.
 template <class T>
 struct Row {
@@ -23,8 +32,8 @@ struct Row {
 // crpcr_kernel.cu:50-55 and :92-98, crNBC.cu:68-73, pcrGauss_kernel.cu:89-98.
 template <class T>
 __device__ __forceinline__ Row<T> reduce_row(const Row<T>& me, const Row<T>& L, const Row<T>& R) {
-  T tmp1 = me.a / L.b;
-  T tmp2 = me.c / R.b;
+  T tmp1 = tdiv(me.a, L.b);
+  T tmp2 = tdiv(me.c, R.b);
   Row<T> o;
   o.b = me.b - L.c * tmp1 - R.a * tmp2;
   o.d = me.d - L.d * tmp1 - R.d * tmp2;
@@ -38,12 +47,12 @@ __device__ __forceinline__ Row<T> reduce_row(const Row<T>& me, const Row<T>& L, 
 template <class T>
 __device__ __forceinline__ T solve2_upper(const Row<T>& r1, const Row<T>& r2) {
   T tmp3 = r2.b * r1.b - r1.c * r2.a;
-  return (r2.b * r1.d - r1.c * r2.d) / tmp3;
+  return tdiv(r2.b * r1.d - r1.c * r2.d, tmp3);
 }
 template <class T>
 __device__ __forceinline__ T solve2_lower(const Row<T>& r1, const Row<T>& r2) {
   T tmp3 = r2.b * r1.b - r1.c * r2.a;
-  return (r2.d * r1.b - r1.d * r2.a) / tmp3;
+  return tdiv(r2.d * r1.b - r1.d * r2.a, tmp3);
 }
 
 // Back substitution of one unknown from its solved neighbours
@@ -51,7 +60,7 @@ __device__ __forceinline__ T solve2_lower(const Row<T>& r1, const Row<T>& r2) {
 // left neighbour term.
 template <class T>
 __device__ __forceinline__ T back_row(const Row<T>& r, T xl, T xr, bool first) {
-  return first ? (r.d - r.c * xr) / r.b : (r.d - r.a * xl - r.c * xr) / r.b;
+  return first ? tdiv(r.d - r.c * xr, r.b) : tdiv(r.d - r.a * xl - r.c * xr, r.b);
 }
 
 // ---- warp shuffles of rows -------------------------------------------------

@@ -85,6 +85,64 @@ def crpcrNBC(a, b, c, d, rest_system_size, x=None, system_size=None):
     return _call("crpcr_nbc", a, b, c, d, x, system_size, int(rest_system_size))
 
 
+def pcrGauss(a, b, c, d, gaussian, x=None, system_size=None):
+    """PCR-then-Thomas with `gaussian` interleaved subsystems (pcrGauss_app.cu:164),
+    exact for every power-of-two gaussian."""
+    return _call("pcr_thomas", a, b, c, d, x, system_size, int(gaussian))
+
+
+def solve(a, b, c, d, x=None, system_size=None):
+    """Generic batched solve of any size (partition method, tridi_solve_*)."""
+    return _call("solve", a, b, c, d, x, system_size)
+
+
+def solve_large(a, b, c, d, system_size, num_systems, layout="contiguous", x=None):
+    """Large systems in either layout (tridi_solve_large_*): flat CUDA tensors,
+    layout "contiguous" (s*n + i) or "interleaved" (i*num_systems + s)."""
+    torch = _torch()
+    lay = {"contiguous": 0, "interleaved": 1}[layout]
+    n, m = int(system_size), int(num_systems)
+    ts = (a, b, c, d)
+    for t in ts:
+        if not t.is_cuda or t.numel() != n * m or not t.is_contiguous() or t.dtype != a.dtype:
+            raise ValueError("a, b, c, d must be contiguous CUDA tensors of n*m elements")
+    if x is None:
+        x = torch.empty_like(a)
+    suf = "f32" if a.dtype == torch.float32 else "f64"
+    L = lib()
+    ws_bytes = L.tridi_large_workspace_bytes(n, m, a.element_size())
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=a.device)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
+    fn = getattr(L, f"tridi_solve_large_{suf}")
+    check(fn(*(t.data_ptr() for t in ts), x.data_ptr(), n, m, lay, ws.data_ptr(), ws_bytes, stream),
+          f"tridi_solve_large_{suf}(n={n}, m={m}, {layout})")
+    return x
+
+
+def refine(a, b, c, d, system_size, num_systems, layout="contiguous", tol=1e-10, max_sweeps=10, x=None):
+    """FP32 solves + FP64 residual refinement (tridi_refine_f32).  a..d float32
+    CUDA tensors (flat, n*m), returns (x float64, sweeps, max relative residual).
+    Raises TridiError if the tolerance is not met within max_sweeps."""
+    torch = _torch()
+    lay = {"contiguous": 0, "interleaved": 1}[layout]
+    n, m = int(system_size), int(num_systems)
+    for t in (a, b, c, d):
+        if t.dtype != torch.float32 or not t.is_cuda or t.numel() != n * m or not t.is_contiguous():
+            raise ValueError("a, b, c, d must be contiguous float32 CUDA tensors of n*m elements")
+    if x is None:
+        x = torch.empty(n * m, dtype=torch.float64, device=a.device)
+    L = lib()
+    wsb = L.tridi_refine_workspace_bytes(n, m, lay)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=a.device)
+    sweeps = ctypes.c_int(0)
+    rel = ctypes.c_double(0.0)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
+    check(L.tridi_refine_f32(a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), x.data_ptr(), n, m, lay,
+                             float(tol), int(max_sweeps), ws.data_ptr(), wsb, stream, ctypes.byref(sweeps),
+                             ctypes.byref(rel)), f"tridi_refine_f32(n={n}, m={m}, {layout})")
+    return x, sweeps.value, rel.value
+
+
 def device_status(reset: bool = True) -> int:
     """Synchronises and returns the TRIDI_DEVERR_* bits of the current device."""
     bits = ctypes.c_uint(0)
