@@ -129,8 +129,7 @@ tridi_status tridi_solve_f32(const float *a, const float *b, const float *c, con
 tridi_status tridi_solve_f64(const double *a, const double *b, const double *c, const double *d, double *x,
                              int n, int num_systems, tridi_stream_t stream);
 
-/* Large systems, any n (up to 8704*16 unknowns in FP32, 4608*16 in FP64), in
-   either layout: TRIDI_LAYOUT_CONTIGUOUS (s*n + i) or TRIDI_LAYOUT_INTERLEAVED
+/* Large systems, any n, in either layout: TRIDI_LAYOUT_CONTIGUOUS (s*n + i) or TRIDI_LAYOUT_INTERLEAVED
    (i*num_systems + s, system-fastest).  Three kernels on `stream`: chunk
    elimination, separator-system solve, chunk back substitution.  Needs a
    device workspace of tridi_large_workspace_bytes() bytes (no allocation
@@ -144,6 +143,22 @@ tridi_status tridi_solve_large_f32(const float *a, const float *b, const float *
 tridi_status tridi_solve_large_f64(const double *a, const double *b, const double *c, const double *d, double *x,
                                    long n, long num_systems, int layout, void *workspace, size_t workspace_bytes,
                                    tridi_stream_t stream);
+
+/* Ragged batches (GB300 addition): systems of different sizes, concatenated --
+   system s owns rows [offsets[s], offsets[s+1]) -- solved by one persistent
+   launch driven by a size-bucketed work queue.  Sizes 1 .. 8704.  The plan is
+   built once on the host from the offsets (host array of num_systems + 1
+   entries) and uploaded to a device buffer; solves then replay it (and can be
+   captured in a CUDA graph: the work counter is reset inside the call).
+   a, b, c, d, x: device, 16-byte aligned, at least round_up(total_rows, 4)
+   elements each. */
+tridi_status tridi_ragged_plan_create(const long *offsets, int num_systems, void **plan);
+size_t tridi_ragged_plan_device_bytes(const void *plan);
+int tridi_ragged_plan_items(const void *plan);
+tridi_status tridi_ragged_plan_upload(const void *plan, void *dev_plan, size_t dev_plan_bytes, tridi_stream_t stream);
+tridi_status tridi_ragged_plan_destroy(void *plan);
+tridi_status tridi_ragged_solve_f32(const float *a, const float *b, const float *c, const float *d, float *x,
+                                    const void *plan, void *dev_plan, tridi_stream_t stream);
 
 /* Mixed-precision iterative refinement: FP32 a, b, c, d in, FP64 x out.
    Only the residual r = d - T x and the accumulation x += e run in FP64;

@@ -51,6 +51,12 @@ for _prec in ("f32", "f64"):
                                                    c_size_t, _P])
 _SIGS["tridi_dropin_release"] = (c_int, [])
 _SIGS["tridi_large_workspace_bytes"] = (c_size_t, [ctypes.c_long, ctypes.c_long, c_int])
+_SIGS["tridi_ragged_plan_create"] = (c_int, [_P, c_int, POINTER(c_void_p)])
+_SIGS["tridi_ragged_plan_device_bytes"] = (c_size_t, [_P])
+_SIGS["tridi_ragged_plan_items"] = (c_int, [_P])
+_SIGS["tridi_ragged_plan_upload"] = (c_int, [_P, _P, c_size_t, _P])
+_SIGS["tridi_ragged_plan_destroy"] = (c_int, [_P])
+_SIGS["tridi_ragged_solve_f32"] = (c_int, [_P, _P, _P, _P, _P, _P, _P, _P])
 _SIGS["tridi_refine_workspace_bytes"] = (c_size_t, [ctypes.c_long, ctypes.c_long, c_int])
 _SIGS["tridi_refine_f32"] = (c_int, [_P, _P, _P, _P, _P, ctypes.c_long, ctypes.c_long, c_int, c_double, c_int, _P,
                                      c_size_t, _P, POINTER(c_int), POINTER(c_double)])

@@ -436,8 +436,7 @@ __global__ void __launch_bounds__(MAXT, MINB) hybrid_kernel(HybridParams p) {
       load_vec<T, K>(st + 1 * (size_t)G * n, vb);
       load_vec<T, K>(st + 2 * (size_t)G * n, vc);
       load_vec<T, K>(st + 3 * (size_t)G * n, vd);
-      __syncwarp();
-      if ((tid & 31) == 0) mbar_arrive(&empty[s]);
+      release_stage(&empty[s]);
     } else {
       const long base = sys * n + (long)t * K;
 #pragma unroll

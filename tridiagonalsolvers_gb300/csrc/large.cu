@@ -8,9 +8,11 @@
 //      i*m + s) a warp covers 32 consecutive systems at the same rows, so
 //      every row load is one 128-byte line.
 //   2. large_assemble: separator row j of system s from chunk j's interface
-//      and chunk j+1's first interior row, written contiguously per system;
-//      the P = ceil(n/L) separators of every system are then solved by the
-//      uniform partition solver (partition.cu).
+//      and chunk j+1's first interior row, in the layout of the data.  The
+//      P = ceil(n/L) separators per system form a batch of the same kind,
+//      solved by the uniform partition solver (contiguous, P <= 8704) or by
+//      this scheme again (interleaved, or larger P), down to a one-thread-
+//      per-system Thomas kernel for interleaved batches of <= 256 rows.
 //   3. large_back: each chunk is read and eliminated again and its rows
 //      recovered from the two separators around it.
 // Memory traffic per unknown: inputs read twice (2 x 16 B FP32), x written
@@ -34,16 +36,17 @@ struct LargeParams {
   void* x;
   long n, m;
   long P;       // chunks per system
-  int L;        // rows per chunk
   int layout;   // 0 contiguous, 1 interleaved
-  void* iface;  // 10 arrays of P*m interface values, index j*m + s
-  void* red;    // 4 arrays (stride PMp) of separator rows, index s*P + j
+  void* iface;  // 10 arrays of P*m interface values (stride PMp), same layout as the data
+  void* red;    // 4 arrays (stride PMp): the separator system, same layout as the data
   long PMp;     // P*m rounded up to 64 elements: keeps each array 256-byte aligned
-  void* sol;    // P*m separator solution, index s*P + j
+  void* sol;    // the separator solution (aliases iface), same layout
 };
 
-// Thread -> (system, chunk).  Interleaved: systems fastest (coalesced rows).
-// Contiguous: chunks fastest (a warp walks one system).
+// Thread -> (system, chunk).  Interleaved: systems fastest; contiguous:
+// chunks fastest.  Either way consecutive threads touch consecutive
+// addresses of the interface and separator arrays, whose layout follows the
+// data's: index j*m + s (interleaved) or s*P + j (contiguous).
 __device__ __forceinline__ void large_coords(const LargeParams& p, long gid, long* s, long* j) {
   if (p.layout == 1) {
     *s = gid % p.m;
@@ -52,6 +55,9 @@ __device__ __forceinline__ void large_coords(const LargeParams& p, long gid, lon
     *j = gid % p.P;
     *s = gid / p.P;
   }
+}
+__device__ __forceinline__ long sep_index(const LargeParams& p, long s, long j) {
+  return p.layout == 1 ? j * p.m + s : s * p.P + j;
 }
 
 template <class T, int L>
@@ -65,35 +71,36 @@ __global__ void __launch_bounds__(256) large_reduce_kernel(LargeParams p) {
   const long rs = p.layout == 1 ? p.m : 1;
   const long base = p.layout == 1 ? r0 * p.m + s : s * p.n + r0;
   Chunk<T, L> ch;
-  chunk_eliminate<T, L>(ch, k, j == 0, j == p.P - 1, static_cast<const T*>(p.a) + base,
+  chunk_eliminate<T, L, true>(ch, k, j == 0, j == p.P - 1, static_cast<const T*>(p.a) + base,
                         static_cast<const T*>(p.b) + base, static_cast<const T*>(p.c) + base,
                         static_cast<const T*>(p.d) + base, rs);
   T* f = static_cast<T*>(p.iface);
-  const long PM = p.P * p.m, o = j * p.m + s;
-  f[0 * PM + o] = ch.fD; f[1 * PM + o] = ch.fC; f[2 * PM + o] = ch.fA;
-  f[3 * PM + o] = ch.lD; f[4 * PM + o] = ch.lC; f[5 * PM + o] = ch.lA;
-  f[6 * PM + o] = ch.sep.a; f[7 * PM + o] = ch.sep.b; f[8 * PM + o] = ch.sep.c; f[9 * PM + o] = ch.sep.d;
+  const long S = p.PMp, o = sep_index(p, s, j);
+  f[0 * S + o] = ch.fD; f[1 * S + o] = ch.fC; f[2 * S + o] = ch.fA;
+  f[3 * S + o] = ch.lD; f[4 * S + o] = ch.lC; f[5 * S + o] = ch.lA;
+  f[6 * S + o] = ch.sep.a; f[7 * S + o] = ch.sep.b; f[8 * S + o] = ch.sep.c; f[9 * S + o] = ch.sep.d;
 }
 
 template <class T>
 __global__ void __launch_bounds__(256) large_assemble_kernel(LargeParams p) {
   const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= p.P * p.m) return;
-  const long s = gid % p.m, j = gid / p.m;  // coalesced interface reads
+  long s, j;
+  large_coords(p, gid, &s, &j);
   const T* f = static_cast<const T*>(p.iface);
-  const long PM = p.P * p.m, o = j * p.m + s;
+  const long S = p.PMp, o = sep_index(p, s, j);
   T nD = T(0), nC = T(0), nA = T(0);
   if (j + 1 < p.P) {
-    nD = f[0 * PM + o + p.m]; nC = f[1 * PM + o + p.m]; nA = f[2 * PM + o + p.m];
+    const long o1 = sep_index(p, s, j + 1);
+    nD = f[0 * S + o1]; nC = f[1 * S + o1]; nA = f[2 * S + o1];
   }
-  const T lD = f[3 * PM + o], lC = f[4 * PM + o], lA = f[5 * PM + o];
-  const T sa = f[6 * PM + o], sb = f[7 * PM + o], sc = f[8 * PM + o], sd = f[9 * PM + o];
+  const T lD = f[3 * S + o], lC = f[4 * S + o], lA = f[5 * S + o];
+  const T sa = f[6 * S + o], sb = f[7 * S + o], sc = f[8 * S + o], sd = f[9 * S + o];
   T* r = static_cast<T*>(p.red);
-  const long q = s * p.P + j, PMp = p.PMp;
-  r[0 * PMp + q] = -sa * lA;
-  r[1 * PMp + q] = sb - sa * lC - sc * nA;
-  r[2 * PMp + q] = -sc * nC;
-  r[3 * PMp + q] = sd - sa * lD - sc * nD;
+  r[0 * S + o] = -sa * lA;
+  r[1 * S + o] = sb - sa * lC - sc * nA;
+  r[2 * S + o] = -sc * nC;
+  r[3 * S + o] = sd - sa * lD - sc * nD;
 }
 
 template <class T, int L>
@@ -107,12 +114,12 @@ __global__ void __launch_bounds__(256) large_back_kernel(LargeParams p) {
   const long rs = p.layout == 1 ? p.m : 1;
   const long base = p.layout == 1 ? r0 * p.m + s : s * p.n + r0;
   Chunk<T, L> ch;
-  chunk_eliminate<T, L>(ch, k, j == 0, j == p.P - 1, static_cast<const T*>(p.a) + base,
+  chunk_eliminate<T, L, true>(ch, k, j == 0, j == p.P - 1, static_cast<const T*>(p.a) + base,
                         static_cast<const T*>(p.b) + base, static_cast<const T*>(p.c) + base,
                         static_cast<const T*>(p.d) + base, rs);
   const T* sol = static_cast<const T*>(p.sol);
-  const T sj = sol[s * p.P + j];
-  const T sl = j > 0 ? sol[s * p.P + j - 1] : T(0);
+  const T sj = sol[sep_index(p, s, j)];
+  const T sl = j > 0 ? sol[sep_index(p, s, j - 1)] : T(0);
   T x[L];
   chunk_back<T, L>(ch, k, sj, sl, x);
   T* gx = static_cast<T*>(p.x) + base;
@@ -121,15 +128,49 @@ __global__ void __launch_bounds__(256) large_back_kernel(LargeParams p) {
     if (i < k) gx[i * rs] = x[i];
 }
 
+// Base case for interleaved systems: one thread per system runs the gold
+// Thomas recurrence (tridiagonal_gold.h:26-44, a[0] and c[n-1] ignored),
+// keeping c' and d' in a scratch array; a warp reads 32 consecutive systems,
+// so every row access is coalesced.
+template <class T>
+__global__ void __launch_bounds__(256) thomas_interleaved_kernel(const T* a, const T* b, const T* c, const T* d,
+                                                                 T* x, long n, long m, T* cp, T* dp) {
+  const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= m) return;
+  T cprev = T(0), dprev = T(0);
+  for (long i = 0; i < n; ++i) {
+    const long k = i * m + s;
+    const T ai = i == 0 ? T(0) : a[k];
+    const T ci = i == n - 1 ? T(0) : c[k];
+    const T inv = tdiv(T(1), b[k] - ai * cprev);
+    cprev = ci * inv;
+    dprev = (d[k] - ai * dprev) * inv;
+    cp[k] = cprev;
+    dp[k] = dprev;
+  }
+  T xn = dprev;
+  x[(n - 1) * m + s] = xn;
+  for (long i = n - 2; i >= 0; --i) {
+    const long k = i * m + s;
+    xn = dp[k] - cp[k] * xn;
+    x[k] = xn;
+  }
+}
+
 namespace {
 constexpr int kChunk = 16;
+constexpr long kThomasMax = 256;  // interleaved base case
 
 long round64(long v) { return (v + 63) & ~63L; }
 
+// Workspace of one level plus the levels below it.
 template <class T>
-size_t large_ws_bytes(long n, long m) {
+size_t large_ws_bytes(long n, long m, int layout) {
+  if (layout == 1 && n <= kThomasMax) return (size_t)2 * round64(n * m) * sizeof(T) + 256;
   const long P = (n + kChunk - 1) / kChunk;
-  return (size_t)(10 * P * m + 4 * round64(P * m)) * sizeof(T) + 1024;
+  size_t own = (size_t)14 * round64(P * m) * sizeof(T) + 256;
+  if (layout == 1 || P > 8704) own += large_ws_bytes<T>(P, m, layout);
+  return own;
 }
 }  // namespace
 
@@ -138,30 +179,41 @@ tridi_status large_solve_device(const T* a, const T* b, const T* c, const T* d, 
                                 void* ws, size_t ws_bytes, tridi_stream_t stream) {
   if (!a || !b || !c || !d || !x || m <= 0 || n <= 0 || (layout != 0 && layout != 1))
     return TRIDI_ERROR_INVALID_VALUE;
-  const long P = (n + kChunk - 1) / kChunk;
-  const int pmax = sizeof(T) == 4 ? 8704 : 4608;
-  if (P > pmax || P * m > (1L << 31)) return TRIDI_ERROR_UNSUPPORTED_SIZE;
-  if (!ws || ws_bytes < large_ws_bytes<T>(n, m)) return TRIDI_ERROR_WORKSPACE_TOO_SMALL;
+  if (n * m > (1L << 34)) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  if (!ws || ws_bytes < large_ws_bytes<T>(n, m, layout)) return TRIDI_ERROR_WORKSPACE_TOO_SMALL;
   if (!current_device()) return TRIDI_ERROR_CUDA;
+  cudaStream_t st = as_stream(stream);
+  char* w = static_cast<char*>(ws);
+  if (layout == 1 && n <= kThomasMax) {
+    T* cp = reinterpret_cast<T*>(w);
+    T* dp = cp + round64(n * m);
+    thomas_interleaved_kernel<T><<<(unsigned)((m + 255) / 256), 256, 0, st>>>(a, b, c, d, x, n, m, cp, dp);
+    return cuda_status(cudaGetLastError());
+  }
   LargeParams p{};
   p.a = a; p.b = b; p.c = c; p.d = d; p.x = x;
-  p.n = n; p.m = m; p.P = P; p.L = kChunk; p.layout = layout;
-  const long PM = P * m;
+  p.n = n; p.m = m; p.layout = layout;
+  p.P = (n + kChunk - 1) / kChunk;
+  const long PM = p.P * m;
   p.PMp = round64(PM);
-  char* w = static_cast<char*>(ws);
-  const size_t ifb = ((size_t)10 * PM * sizeof(T) + 255) & ~size_t(255);
   p.iface = w;
-  p.red = w + ifb;
+  p.red = w + (size_t)10 * p.PMp * sizeof(T);
   p.sol = w;  // the interface is dead once the separator rows are assembled
-  cudaStream_t st = as_stream(stream);
+  void* inner = w + (size_t)14 * p.PMp * sizeof(T) + 256;
+  const size_t inner_bytes = ws_bytes - ((size_t)14 * p.PMp * sizeof(T) + 256);
   const unsigned blocks = (unsigned)((PM + 255) / 256);
   large_reduce_kernel<T, kChunk><<<blocks, 256, 0, st>>>(p);
   large_assemble_kernel<T><<<blocks, 256, 0, st>>>(p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e);
   const T* r = static_cast<const T*>(p.red);
-  tridi_status ts = partition_solve_device<T>(r, r + p.PMp, r + 2 * p.PMp, r + 3 * p.PMp, static_cast<T*>(p.sol),
-                                              (int)P, (int)m, stream);
+  tridi_status ts;
+  if (layout == 0 && p.P <= 8704 / (sizeof(T) == 4 ? 1 : 2))
+    ts = partition_solve_device<T>(r, r + p.PMp, r + 2 * p.PMp, r + 3 * p.PMp, static_cast<T*>(p.sol), (int)p.P,
+                                   (int)m, stream);
+  else
+    ts = large_solve_device<T>(r, r + p.PMp, r + 2 * p.PMp, r + 3 * p.PMp, static_cast<T*>(p.sol), p.P, m, layout,
+                               inner, inner_bytes, stream);
   if (ts != TRIDI_SUCCESS) return ts;
   large_back_kernel<T, kChunk><<<blocks, 256, 0, st>>>(p);
   return cuda_status(cudaGetLastError());
@@ -177,8 +229,12 @@ template tridi_status large_solve_device<double>(const double*, const double*, c
 extern "C" {
 
 size_t tridi_large_workspace_bytes(long n, long num_systems, int elem_size) {
-  return elem_size == 8 ? tridi::large_ws_bytes<double>(n, num_systems)
-                        : tridi::large_ws_bytes<float>(n, num_systems);
+  // the larger of the two layouts' needs, so one query serves both
+  const size_t c0 = elem_size == 8 ? tridi::large_ws_bytes<double>(n, num_systems, 0)
+                                   : tridi::large_ws_bytes<float>(n, num_systems, 0);
+  const size_t c1 = elem_size == 8 ? tridi::large_ws_bytes<double>(n, num_systems, 1)
+                                   : tridi::large_ws_bytes<float>(n, num_systems, 1);
+  return c0 > c1 ? c0 : c1;
 }
 tridi_status tridi_solve_large_f32(const float* a, const float* b, const float* c, const float* d, float* x, long n,
                                    long m, int layout, void* ws, size_t ws_bytes, tridi_stream_t s) {

@@ -257,8 +257,7 @@ __global__ void __launch_bounds__(MAXT) nbc_kernel(NbcParams p) {
     }
     if (sys < p.m) nbc_solve<T>(la, lb, lc, ld, W, gx + sys * n, n, p.rest, vec0, p.vec != 0);
     if (S > 0) {
-      __syncwarp();
-      if ((tid & 31) == 0) mbar_arrive(&empty[s]);
+      release_stage(&empty[s]);
     }
   }
 }

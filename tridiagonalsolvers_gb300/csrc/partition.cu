@@ -142,8 +142,7 @@ __global__ void __launch_bounds__(MAXT, MINB) partition_kernel(PartParams p) {
       chunk_back<T, K>(ch, kr, sj, sl, x);
     }
     if (S > 0) {
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[s]);
+      release_stage(&empty[s]);
     }
     if (sys < p.m) {
       T* dst = gx + sys * (long)n + r0;

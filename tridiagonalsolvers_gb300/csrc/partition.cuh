@@ -36,14 +36,27 @@ struct Chunk {
 // Eliminates the lane's k rows (0 <= k <= K), row i of the chunk being
 // (pa[i*rs], pb[i*rs], pc[i*rs], pd[i*rs]).  first/last: the chunk holds the
 // system's first/last row.
-template <class T, int K>
+// PREFETCH (for global-memory rows): all k rows are loaded into registers
+// before the dependent elimination chain starts, so their loads overlap.
+template <class T, int K, bool PREFETCH = false>
 __device__ __forceinline__ void chunk_eliminate(Chunk<T, K>& ch, int k, bool first, bool last, const T* pa,
                                                 const T* pb, const T* pc, const T* pd, long rs = 1) {
+  T qa[PREFETCH ? K : 1], qb[PREFETCH ? K : 1], qc[PREFETCH ? K : 1], qd[PREFETCH ? K : 1];
+  if constexpr (PREFETCH) {
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      if (i < k - 1) {
+        qa[i] = pa[i * rs]; qb[i] = pb[i * rs]; qc[i] = pc[i * rs]; qd[i] = pd[i * rs];
+      }
+    }
+  }
   T cprev = T(0), aprev = T(0), dprev = T(0);
 #pragma unroll
   for (int i = 0; i < K; ++i) {
     if (i < k - 1) {
-      const Row<T> r{pa[i * rs], pb[i * rs], pc[i * rs], pd[i * rs]};
+      const Row<T> r = PREFETCH ? Row<T>{qa[PREFETCH ? i : 0], qb[PREFETCH ? i : 0], qc[PREFETCH ? i : 0],
+                                         qd[PREFETCH ? i : 0]}
+                                : Row<T>{pa[i * rs], pb[i * rs], pc[i * rs], pd[i * rs]};
       const T a = (i == 0 && first) ? T(0) : r.a;
       const T inv = tdiv(T(1), r.b - a * cprev);
       ch.cp[i] = r.c * inv;

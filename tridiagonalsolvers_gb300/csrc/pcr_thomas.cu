@@ -111,8 +111,7 @@ __global__ void __launch_bounds__(MAXT) pcr_thomas_kernel(PTParams p) {
         wc[i] = i == n - 1 ? T(0) : st[2 * (size_t)G * n + i];
         wd[i] = st[3 * (size_t)G * n + i];
       }
-      __syncwarp();
-      if ((tid & 31) == 0) mbar_arrive(&empty[s]);
+      release_stage(&empty[s]);
     } else {
       for (int i = t; i < n; i += tps) {
         wa[i] = i == 0 ? T(0) : ga[src_sys * n + i];

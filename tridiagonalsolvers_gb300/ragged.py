@@ -1,0 +1,65 @@
+"""Ragged batches on the GPU: systems of different sizes in one persistent
+launch (tridi_ragged_* of include/tridi.h).
+
+    plan = RaggedPlan(offsets)          # host int64 array, num_systems + 1 entries
+    x = plan.solve(a, b, c, d)          # flat float32 CUDA tensors, concatenated rows
+
+The plan (size buckets, work items) is built once and reused; `padded(n)`
+gives the allocation length the arrays need (a multiple of 4 elements).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import check, lib
+
+
+def padded(total_rows: int) -> int:
+    return (int(total_rows) + 3) & ~3
+
+
+class RaggedPlan:
+    def __init__(self, offsets, device=None):
+        import torch
+
+        off = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
+        if off.ndim != 1 or len(off) < 2 or off[0] != 0 or np.any(np.diff(off) <= 0):
+            raise ValueError("offsets must start at 0 and increase strictly")
+        self.offsets = off
+        self.num_systems = len(off) - 1
+        self.total_rows = int(off[-1])
+        L = lib()
+        h = ctypes.c_void_p()
+        check(L.tridi_ragged_plan_create(off.ctypes.data, self.num_systems, ctypes.byref(h)), "ragged plan")
+        self._h = h
+        self.items = L.tridi_ragged_plan_items(h)
+        nbytes = L.tridi_ragged_plan_device_bytes(h)
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self._dev = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        check(L.tridi_ragged_plan_upload(h, self._dev.data_ptr(), nbytes, stream), "ragged plan upload")
+
+    def solve(self, a, b, c, d, x=None):
+        import torch
+
+        need = padded(self.total_rows)
+        for t in (a, b, c, d):
+            if t.dtype != torch.float32 or not t.is_cuda or not t.is_contiguous() or t.numel() < need:
+                raise ValueError(f"a, b, c, d must be contiguous float32 CUDA tensors of >= {need} elements")
+        if x is None:
+            x = torch.zeros(need, dtype=torch.float32, device=a.device)
+        stream = ctypes.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
+        check(lib().tridi_ragged_solve_f32(a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), x.data_ptr(),
+                                           self._h, self._dev.data_ptr(), stream), "tridi_ragged_solve_f32")
+        return x
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().tridi_ragged_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
