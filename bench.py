@@ -134,21 +134,15 @@ def dist_init(gpus: int):
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
+    from tridiagonalsolvers_gb300.distributed import barrier as _barrier
 
-        dist.barrier()
+    _barrier()
 
 
 def max_over_ranks(v: float, world: int, device) -> float:
-    if world == 1:
-        return v
-    import torch
-    import torch.distributed as dist
+    from tridiagonalsolvers_gb300.distributed import max_over_ranks as _max
 
-    t = torch.tensor([v], dtype=torch.float64, device=device)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return _max(v, device)
 
 
 # ---------------------------------------------------------------------------
