@@ -175,6 +175,23 @@ tridi_status tridi_refine_f32(const float *a, const float *b, const float *c, co
                               long num_systems, int layout, double tol, int max_sweeps, void *workspace,
                               size_t workspace_bytes, tridi_stream_t stream, int *sweeps, double *rel_residual);
 
+/* Allocation-free solve (no counterpart in the reference): for callers that
+   cannot call cudaMalloc at solve time, e.g. an application whose device
+   memory is all owned by its own pool, or a latency-critical loop that must
+   not pay an allocation's implicit synchronisation.  Interleaved layout
+   (element i of system s at i*num_systems + s), one thread per system runs
+   the Thomas recurrence; its forward-sweep coefficients live in a 16 MiB
+   array compiled into the library, so n * num_systems must not exceed
+   tridi_noalloc_max_unknowns() (2^21); larger requests return
+   TRIDI_ERROR_WORKSPACE_TOO_SMALL.  The array is shared by all calls on a
+   device: calls that overlap on the GPU race on it.  The first call on a
+   device looks up the array's address; make it before any stream capture.
+   CUDA errors are reported by tridi_noalloc_last_cuda_error(). */
+long tridi_noalloc_max_unknowns(void);
+int tridi_noalloc_last_cuda_error(void);
+tridi_status tridi_solve_interleaved_noalloc_f32(const float *a, const float *b, const float *c, const float *d,
+                                                 float *x, long n, long num_systems, tridi_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
