@@ -402,6 +402,53 @@ def run_large(args):
     return 0
 
 
+def run_ragged(args):
+    """100000 ADI line systems, sizes log-uniform in [32, 8192]: one persistent
+    launch (size-bucketed work queue), plain FP32 and FP32 + FP64-residual
+    refinement captured in a CUDA graph."""
+    import torch
+
+    from tridiagonalsolvers_gb300 import workloads
+    from tridiagonalsolvers_gb300.ragged import RaggedPlan, RaggedRefiner, padded
+
+    dev = torch.device("cuda", 0)
+    count = args.ragged_count
+    sizes = workloads.ragged_sizes(count, 32, 8192, seed=workloads.SEEDS["c4"])
+    a, b, c, d, off = workloads.adi(sizes, seed=workloads.SEEDS["c4"])
+    total = int(off[-1])
+
+    def up(v):
+        t = torch.zeros(padded(total), dtype=torch.float32, device=dev)
+        t[:total] = torch.from_numpy(v)
+        return t
+
+    t = [up(v) for v in (a, b, c, d)]
+    del a, b, c, d
+    plan = RaggedPlan(off, device=dev)
+    x = torch.zeros(padded(total), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ms = time_kernel(lambda: plan.solve(*t, x=x), stream, args.warmup, args.steps)
+    ref = RaggedRefiner(plan, *t, sweeps=args.sweeps, graph=True)
+    rms = time_kernel(ref.launch, stream, 2, max(2, args.steps // 2))
+    x64, rel = ref.run()
+    peak, kind = measured_peaks()
+    line = {
+        "metric": METRIC, "value": total / (ms * 1e-3), "unit": "unknowns/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"ragged ADI batch, {count} systems, sizes log-uniform in [32, 8192]",
+                   "total_unknowns": total, "work_items": plan.items, "seed": workloads.SEEDS["c4"],
+                   "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "achieved": BYTES_PER_UNKNOWN * total / (ms * 1e-3) / 1e9, "peak": peak,
+                     "unit": "GB/s", "frac": BYTES_PER_UNKNOWN * total / (ms * 1e-3) / 1e9 / peak,
+                     "peak_source": kind, "traffic": None},
+        "refined": {"value": total / (rms * 1e-3), "ms_per_step": rms, "sweeps": args.sweeps, "rel_residual": rel,
+                    "tol": 1e-10, "frac_of_plain": ms / rms, "cuda_graph": True},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -410,8 +457,11 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-table", action="store_true", help="skip the per-kernel table")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--workload", default="batch", choices=["batch", "large"],
-                    help="batch: 65536 x 256 (default, the headline); large: 1024 x 65536 interleaved")
+    ap.add_argument("--workload", default="batch", choices=["batch", "large", "ragged"],
+                    help="batch: 65536 x 256 (default, the headline); large: 1024 x 65536 interleaved; "
+                         "ragged: 100000 ADI systems of 32..8192 unknowns")
+    ap.add_argument("--ragged-count", type=int, default=100000, help="systems of the ragged workload")
+    ap.add_argument("--sweeps", type=int, default=1, help="refinement sweeps of the ragged workload")
     ap.add_argument("--large-n", type=int, default=65536, help="system size of the large workload")
     ap.add_argument("--no-refine", action="store_true", help="large workload: plain solve only")
     args = ap.parse_args()
@@ -421,6 +471,8 @@ def main():
         return run_reference(args)
     if args.workload == "large":
         return run_large(args)
+    if args.workload == "ragged":
+        return run_ragged(args)
     return run_gpu(args)
 
 

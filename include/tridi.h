@@ -65,6 +65,7 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
    autotuner and by experiments; they never change results, only speed. */
 #define TRIDI_TUNE_STAGES 1     /* cp.async.bulk pipeline stages per CTA (1..8) */
 #define TRIDI_TUNE_CRPCR_REST 2 /* switch level of the CR-PCR correction solves */
+#define TRIDI_TUNE_CR_ROWS 3    /* rows per thread of the CR/PCR/CR-PCR kernels (2, 4, 8, 16) */
 tridi_status tridi_set_tunable(int key, int value);
 int tridi_get_tunable(int key);
 
@@ -146,7 +147,7 @@ tridi_status tridi_solve_large_f64(const double *a, const double *b, const doubl
 
 /* Ragged batches (GB300 addition): systems of different sizes, concatenated --
    system s owns rows [offsets[s], offsets[s+1]) -- solved by one persistent
-   launch driven by a size-bucketed work queue.  Sizes 1 .. 8704.  The plan is
+   launch driven by a size-bucketed work queue.  Sizes 1 .. 17408.  The plan is
    built once on the host from the offsets (host array of num_systems + 1
    entries) and uploaded to a device buffer; solves then replay it (and can be
    captured in a CUDA graph: the work counter is reset inside the call).
@@ -155,10 +156,22 @@ tridi_status tridi_solve_large_f64(const double *a, const double *b, const doubl
 tridi_status tridi_ragged_plan_create(const long *offsets, int num_systems, void **plan);
 size_t tridi_ragged_plan_device_bytes(const void *plan);
 int tridi_ragged_plan_items(const void *plan);
+long tridi_ragged_plan_total_rows(const void *plan);
+int tridi_ragged_plan_num_systems(const void *plan);
 tridi_status tridi_ragged_plan_upload(const void *plan, void *dev_plan, size_t dev_plan_bytes, tridi_stream_t stream);
 tridi_status tridi_ragged_plan_destroy(void *plan);
 tridi_status tridi_ragged_solve_f32(const float *a, const float *b, const float *c, const float *d, float *x,
                                     const void *plan, void *dev_plan, tridi_stream_t stream);
+/* Ragged FP32 solves with FP64 residual and FP64 accumulation, a fixed number
+   of correction sweeps and no host synchronisation (capturable in a CUDA
+   graph).  x: FP64, round_up(total_rows, 4) elements.  offsets_dev: the
+   plan's offsets in device memory.  *dev_rel (device) receives the final
+   maximum relative residual ||d - T x|| / ||d||. */
+size_t tridi_ragged_refine_workspace_bytes(long total_rows, long num_systems);
+tridi_status tridi_ragged_refine_f32(const float *a, const float *b, const float *c, const float *d, double *x,
+                                     const void *plan, void *dev_plan, const long *offsets_dev, int sweeps,
+                                     void *workspace, size_t workspace_bytes, double *dev_rel,
+                                     tridi_stream_t stream);
 
 /* Mixed-precision iterative refinement: FP32 a, b, c, d in, FP64 x out.
    Only the residual r = d - T x and the accumulation x += e run in FP64;

@@ -71,3 +71,41 @@ def test_ragged_full_workload_100000_systems(cuda):
     assert np.all(np.isfinite(x))
     rng = np.random.default_rng(0)
     _check_systems(a, b, c, d, x, off, rng.choice(len(sizes), 300, replace=False))
+
+
+def test_ragged_refined_graph_replay(cuda):
+    """Refinement of a ragged batch (systems up to 16384 rows, beyond shared
+    memory) to 1e-10, captured once in a CUDA graph; replays agree bit for bit
+    with the eager sequence and with the FP64 oracle."""
+    from tridiagonalsolvers_gb300.ragged import RaggedRefiner
+
+    rng = np.random.default_rng(3)
+    sizes = np.concatenate([rng.integers(32, 480, 200), rng.integers(480, 8704, 40), rng.integers(8705, 16385, 6),
+                            [16384, 17408]])
+    a, b, c, d, off = workloads.adi(sizes, seed=5)
+    total = int(off[-1])
+    t = [_dev(cuda, v, total) for v in (a, b, c, d)]
+    plan = RaggedPlan(off)
+    eager = RaggedRefiner(plan, *t, sweeps=1, graph=False)
+    xe, rel_e = eager.run()
+    xe = xe.cpu().numpy()[:total].copy()
+    g = RaggedRefiner(plan, *t, sweeps=1, graph=True)
+    for _ in range(2):
+        xg, rel_g = g.run()
+        assert np.array_equal(xg.cpu().numpy()[:total], xe)
+        assert rel_g == rel_e
+    assert rel_e <= 1e-10, f"max relative residual {rel_e:.2e} after one sweep"
+    rng2 = np.random.default_rng(1)
+    for s in list(rng2.choice(len(sizes), 40, replace=False)) + [len(sizes) - 1, len(sizes) - 2]:
+        lo, hi = off[s], off[s + 1]
+        sl = [v[lo:hi][None] for v in (a, b, c, d)]
+        res = gold.rel_residual(*sl, xe[lo:hi][None])[0]
+        assert res <= 1.5e-10, f"system {s} (n={hi - lo}) oracle residual {res:.2e}"
+
+
+def test_ragged_big_systems_plain(cuda):
+    sizes = np.array([8705, 12000, 16384, 17408, 100, 9000])
+    a, b, c, d, off = workloads.adi(sizes, seed=8)
+    total = int(off[-1])
+    x = RaggedPlan(off).solve(*(_dev(cuda, v, total) for v in (a, b, c, d))).cpu().numpy()[:total]
+    _check_systems(a, b, c, d, x, off, range(len(sizes)))

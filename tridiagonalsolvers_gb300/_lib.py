@@ -57,6 +57,10 @@ _SIGS["tridi_ragged_plan_items"] = (c_int, [_P])
 _SIGS["tridi_ragged_plan_upload"] = (c_int, [_P, _P, c_size_t, _P])
 _SIGS["tridi_ragged_plan_destroy"] = (c_int, [_P])
 _SIGS["tridi_ragged_solve_f32"] = (c_int, [_P, _P, _P, _P, _P, _P, _P, _P])
+_SIGS["tridi_ragged_plan_total_rows"] = (ctypes.c_long, [_P])
+_SIGS["tridi_ragged_plan_num_systems"] = (c_int, [_P])
+_SIGS["tridi_ragged_refine_workspace_bytes"] = (c_size_t, [ctypes.c_long, ctypes.c_long])
+_SIGS["tridi_ragged_refine_f32"] = (c_int, [_P, _P, _P, _P, _P, _P, _P, _P, c_int, _P, c_size_t, _P, _P])
 _SIGS["tridi_noalloc_max_unknowns"] = (ctypes.c_long, [])
 _SIGS["tridi_noalloc_last_cuda_error"] = (c_int, [])
 _SIGS["tridi_solve_interleaved_noalloc_f32"] = (c_int, [_P, _P, _P, _P, _P, ctypes.c_long, ctypes.c_long, _P])

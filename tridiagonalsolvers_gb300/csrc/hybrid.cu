@@ -27,6 +27,13 @@ bool choose_shape(int n, Shape* s) {
     if (n > 2048) return false;
     K = n <= 8 ? n / 2 : (n == 2048 ? 8 : 4);
   }
+  const int tk = tunable(TRIDI_TUNE_CR_ROWS);
+  if (tk > 0 && is_pow2(tk) && tk <= n / 2 && n / tk <= 256) {
+    // only shapes with an instantiated kernel (see solve_hybrid)
+    const bool warp = n / tk <= 32;
+    const bool have = sizeof(T) == 4 ? (warp ? tk <= 16 : (tk == 8 || tk == 16)) : (warp ? tk <= 4 : (tk == 4 || tk == 8));
+    if (have) K = tk;
+  }
   s->K = K;
   s->tps = n / K;
   s->warp = s->tps <= 32;

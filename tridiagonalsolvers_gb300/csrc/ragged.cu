@@ -7,6 +7,11 @@
 //   MULTI  up to 16 systems of <= 480 rows: one warp per system
 //   SINGLE one system of 481 .. kStageRows-3 rows: the whole CTA
 //   DOUBLE one system of up to 8704 rows: the whole CTA, both stage buffers
+//   BIG    one system of up to 17408 rows, read from global memory (no
+//          staging): every thread owns two chunks; pass 1 eliminates them
+//          and exports their interfaces, the 1024 separators are solved by
+//          PCR in shared memory, pass 2 eliminates again (rows now in L2)
+//          and substitutes back
 // One CTA per SM (512 consumer threads + a producer warp).  The producer
 // claims the next item with an atomicAdd on a counter in the plan buffer,
 // stages it into one of two shared-memory buffers with cp.async.bulk (each
@@ -31,9 +36,11 @@ constexpr int kRagWarps = kRagThreads / 32;
 constexpr int kStageRows = 6144;       // rows per stage buffer (per array)
 constexpr int kWarpMaxRows = 480;      // MULTI systems: 32 lanes x 15 rows
 constexpr int kMaxItemSystems = 16;
-constexpr int kMaxSystemRows = 17 * kRagThreads;  // 8704
+constexpr int kMaxSystemRows = 17 * kRagThreads;  // 8704: largest staged system
+constexpr int kBigChunks = 2;                      // chunks per thread for BIG systems
+constexpr int kMaxBigRows = kBigChunks * 17 * kRagThreads;  // 17408
 
-enum ItemKind : int { kMulti = 0, kSingle = 1, kDouble = 2, kNop = 3, kCont = 4, kEnd = 5 };
+enum ItemKind : int { kMulti = 0, kSingle = 1, kDouble = 2, kNop = 3, kCont = 4, kEnd = 5, kBig = 6 };
 
 struct RagItem {
   int kind;
@@ -78,9 +85,11 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
   float* buf = reinterpret_cast<float*>(smem + 64 + 2 * sizeof(RagStage) + 64 - ((64 + 2 * sizeof(RagStage)) % 64));
   // buf layout: array q (a, b, c, d) occupies [q * 2 * kStageRows, (q+1) * 2 * kStageRows);
   // stage s is the half [s * kStageRows, (s+1) * kStageRows) of every array.
-  float* Rsh = buf + 4 * 2 * kStageRows;  // CTA-mode separators: 4 x kRagThreads
-  float* Xsh = Rsh + 4 * kRagThreads;     // their solution
-  float* F0 = Xsh + kRagThreads;          // lane-0 first-row coefficients of each warp (3 x kRagWarps)
+  constexpr int kSepRows = kBigChunks * kRagThreads;
+  float* Rsh = buf + 4 * 2 * kStageRows;  // CTA-mode separators: 4 x kSepRows
+  float* Xsh = Rsh + 4 * kSepRows;        // their solution
+  float* F0 = Xsh + kSepRows;             // lane-0 first-row coefficients of each warp (3 x kRagWarps)
+  float* Fb = F0 + 3 * kRagWarps;         // BIG: first-row coefficients of every chunk (3 x kSepRows)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if (tid == 0) {
@@ -117,6 +126,11 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
         mbar_arrive(&full[s]);
         done = true;
         break;
+      }
+      if (kind == kBig) {  // rows are read from global memory by the consumers
+        mbar_arrive(&full[s]);
+        ++k;
+        continue;
       }
       const RagItem it = p.items[item];
       // Bytes of the whole item first: the single arrive carries the full
@@ -228,6 +242,87 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
       for (int i = 0; i < KC; ++i)
         if (i < kr) dst[i] = xr[i];
       consumer_sync(kRagThreads);  // F0 / Xsh reused by the next item
+    } else if (kind == kBig) {
+      const RagItem it = p.items[desc[s].item];
+      const RagSys sy = p.sys[it.first];
+      const int n = sy.n;
+      constexpr int KC = 17;
+      constexpr int NS = kSepRows;  // chunks (= separators) of the system
+      const int kk = odd_ceil_dev((n + NS - 1) / NS);
+      const float* ga = p.a + sy.off;
+      const float* gb = p.b + sy.off;
+      const float* gc = p.c + sy.off;
+      const float* gd = p.d + sy.off;
+      // pass 1: eliminate both chunks, export first-row coefficients to shared
+      // memory and keep the last-row coefficients and separator rows
+      Row<float> sep[kBigChunks];
+      float lD[kBigChunks], lC[kBigChunks], lA[kBigChunks];
+#pragma unroll
+      for (int q = 0; q < kBigChunks; ++q) {
+        const int j = q * kRagThreads + tid;
+        const int r0 = j * kk;
+        int kr = n - r0;
+        kr = kr < 0 ? 0 : (kr > kk ? kk : kr);
+        Chunk<float, KC> ch;
+        chunk_eliminate<float, KC>(ch, kr, j == 0, r0 + kr == n && kr > 0, ga + r0, gb + r0, gc + r0,
+                                         gd + r0);
+        Fb[3 * j + 0] = ch.fD; Fb[3 * j + 1] = ch.fC; Fb[3 * j + 2] = ch.fA;
+        sep[q] = ch.sep; lD[q] = ch.lD; lC[q] = ch.lC; lA[q] = ch.lA;
+      }
+      consumer_sync(kRagThreads);
+      // separator rows; PCR over all NS of them, kBigChunks rows per thread
+      Row<float> sr[kBigChunks];
+#pragma unroll
+      for (int q = 0; q < kBigChunks; ++q) {
+        const int j = q * kRagThreads + tid;
+        const float nD = j + 1 < NS ? Fb[3 * (j + 1) + 0] : 0.f;
+        const float nC = j + 1 < NS ? Fb[3 * (j + 1) + 1] : 0.f;
+        const float nA = j + 1 < NS ? Fb[3 * (j + 1) + 2] : 0.f;
+        const Row<float>& e = sep[q];
+        sr[q] = Row<float>{-e.a * lA[q], e.b - e.a * lC[q] - e.c * nA, -e.c * nC, e.d - e.a * lD[q] - e.c * nD};
+      }
+      const Row<float> id{0.f, 1.f, 0.f, 0.f};
+      for (int dl = 1; dl < NS; dl *= 2) {
+#pragma unroll
+        for (int q = 0; q < kBigChunks; ++q) {
+          const int j = q * kRagThreads + tid;
+          Rsh[j] = sr[q].a; Rsh[NS + j] = sr[q].b; Rsh[2 * NS + j] = sr[q].c; Rsh[3 * NS + j] = sr[q].d;
+        }
+        consumer_sync(kRagThreads);
+#pragma unroll
+        for (int q = 0; q < kBigChunks; ++q) {
+          const int j = q * kRagThreads + tid;
+          const Row<float> L = j >= dl ? Row<float>{Rsh[j - dl], Rsh[NS + j - dl], Rsh[2 * NS + j - dl],
+                                                    Rsh[3 * NS + j - dl]}
+                                       : id;
+          const Row<float> R = j + dl < NS ? Row<float>{Rsh[j + dl], Rsh[NS + j + dl], Rsh[2 * NS + j + dl],
+                                                        Rsh[3 * NS + j + dl]}
+                                           : id;
+          sr[q] = reduce_row(sr[q], L, R);
+        }
+        consumer_sync(kRagThreads);
+      }
+#pragma unroll
+      for (int q = 0; q < kBigChunks; ++q) Xsh[q * kRagThreads + tid] = tdiv(sr[q].d, sr[q].b);
+      consumer_sync(kRagThreads);
+      // pass 2: eliminate again and substitute back
+#pragma unroll
+      for (int q = 0; q < kBigChunks; ++q) {
+        const int j = q * kRagThreads + tid;
+        const int r0 = j * kk;
+        int kr = n - r0;
+        kr = kr < 0 ? 0 : (kr > kk ? kk : kr);
+        Chunk<float, KC> ch;
+        chunk_eliminate<float, KC>(ch, kr, j == 0, r0 + kr == n && kr > 0, ga + r0, gb + r0, gc + r0,
+                                         gd + r0);
+        float xr[KC];
+        chunk_back<float, KC>(ch, kr, Xsh[j], j > 0 ? Xsh[j - 1] : 0.f, xr);
+        float* dst = p.x + sy.off + r0;
+#pragma unroll
+        for (int i = 0; i < KC; ++i)
+          if (i < kr) dst[i] = xr[i];
+      }
+      consumer_sync(kRagThreads);  // Fb / Xsh reused by the next item
     }
     release_stage(&empty[s]);
   }
@@ -249,7 +344,8 @@ namespace {
 size_t rag_smem_bytes() {
   size_t head = 64 + 2 * sizeof(RagStage);
   head += 64 - head % 64;
-  return head + (size_t)(4 * 2 * kStageRows + 5 * kRagThreads + 3 * kRagWarps) * sizeof(float);
+  return head + (size_t)(4 * 2 * kStageRows + 5 * kBigChunks * kRagThreads + 3 * kRagWarps +
+                         3 * kBigChunks * kRagThreads) * sizeof(float);
 }
 long padded_rows(long off, int n) { return ((off + n + 3) & ~3L) - (off & ~3L); }
 }  // namespace
@@ -269,7 +365,7 @@ tridi_status tridi_ragged_plan_create(const long* offsets, int num_systems, void
   std::vector<int> order(num_systems);
   for (int s = 0; s < num_systems; ++s) {
     const long n = offsets[s + 1] - offsets[s];
-    if (n <= 0 || n > kMaxSystemRows || padded_rows(offsets[s], (int)n) > 2 * kStageRows) {
+    if (n <= 0 || n > kMaxBigRows) {
       delete plan;
       return TRIDI_ERROR_UNSUPPORTED_SIZE;
     }
@@ -285,6 +381,11 @@ tridi_status tridi_ragged_plan_create(const long* offsets, int num_systems, void
   while (i < num_systems) {
     const RagSys& sy = plan->sys[i];
     const long pr = padded_rows(sy.off, sy.n);
+    if (sy.n > kMaxSystemRows || pr > 2 * kStageRows) {
+      plan->items.push_back(RagItem{(int)kBig, 1, i, 0});
+      ++i;
+      continue;
+    }
     if (sy.n > kWarpMaxRows) {
       RagItem it{pr > kStageRows ? (int)kDouble : (int)kSingle, 1, i, (int)pr};
       plan->items.push_back(it);
@@ -308,6 +409,14 @@ tridi_status tridi_ragged_plan_create(const long* offsets, int num_systems, void
 
 size_t tridi_ragged_plan_device_bytes(const void* plan) {
   return plan ? static_cast<const RaggedPlan*>(plan)->device_bytes() : 0;
+}
+
+long tridi_ragged_plan_total_rows(const void* plan) {
+  return plan ? static_cast<const RaggedPlan*>(plan)->total_rows : 0;
+}
+
+int tridi_ragged_plan_num_systems(const void* plan) {
+  return plan ? static_cast<const RaggedPlan*>(plan)->num_systems : 0;
 }
 
 int tridi_ragged_plan_items(const void* plan) {

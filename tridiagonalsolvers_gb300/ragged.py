@@ -63,3 +63,60 @@ class RaggedPlan:
             except Exception:
                 pass
             self._h = None
+
+
+class RaggedRefiner:
+    """FP32 ragged solves with FP64 residual refinement, a fixed number of
+    correction sweeps, optionally captured once in a CUDA graph and replayed.
+
+        r = RaggedRefiner(plan, a, b, c, d, sweeps=1, graph=True)
+        x64, rel = r.run()       # FP64 solution (padded rows) and max relative residual
+    """
+
+    def __init__(self, plan: RaggedPlan, a, b, c, d, sweeps: int = 1, graph: bool = True):
+        import torch
+
+        L = lib()
+        check(L.tridi_init(), "tridi_init")  # status word allocated outside any capture
+        self.plan, self.sweeps = plan, int(sweeps)
+        self.inputs = (a, b, c, d)
+        dev = a.device
+        need = padded(plan.total_rows)
+        self.x = torch.zeros(need, dtype=torch.float64, device=dev)
+        self.rel = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.off = torch.from_numpy(plan.offsets).to(dev)
+        wsb = L.tridi_ragged_refine_workspace_bytes(plan.total_rows, plan.num_systems)
+        self.ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+        self._wsb = wsb
+        self.graph = None
+        if graph:
+            self._launch()  # warm up: kernel attributes set, everything resident
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, capture_error_mode="relaxed"):
+                self._launch()
+            self.graph = g
+
+    def _launch(self):
+        import torch
+
+        a, b, c, d = self.inputs
+        stream = ctypes.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
+        check(lib().tridi_ragged_refine_f32(a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(),
+                                            self.x.data_ptr(), self.plan._h, self.plan._dev.data_ptr(),
+                                            self.off.data_ptr(), self.sweeps, self.ws.data_ptr(), self._wsb,
+                                            self.rel.data_ptr(), stream), "tridi_ragged_refine_f32")
+
+    def launch(self):
+        """Enqueue one refined solve (graph replay if captured); no sync."""
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._launch()
+
+    def run(self):
+        import torch
+
+        self.launch()
+        torch.cuda.synchronize()
+        return self.x, float(self.rel.item())
