@@ -147,7 +147,7 @@ tridi_status tridi_solve_large_f64(const double *a, const double *b, const doubl
 
 /* Ragged batches (GB300 addition): systems of different sizes, concatenated --
    system s owns rows [offsets[s], offsets[s+1]) -- solved by one persistent
-   launch driven by a size-bucketed work queue.  Sizes 1 .. 17408.  The plan is
+   launch driven by a size-bucketed work queue.  Sizes 1 .. 24480.  The plan is
    built once on the host from the offsets (host array of num_systems + 1
    entries) and uploaded to a device buffer; solves then replay it (and can be
    captured in a CUDA graph: the work counter is reset inside the call).
@@ -172,6 +172,28 @@ tridi_status tridi_ragged_refine_f32(const float *a, const float *b, const float
                                      const void *plan, void *dev_plan, const long *offsets_dev, int sweeps,
                                      void *workspace, size_t workspace_bytes, double *dev_rel,
                                      tridi_stream_t stream);
+
+/* Serving loop with continuous batching (GB300 addition).  Requests are small
+   ragged batches of host arrays (FP32 a, b, c, d; FP64 x out; offsets of
+   num_systems + 1 rows starting at 0); they are admitted in arrival order by
+   their HBM footprint (tridi_server_request_footprint) against
+   hbm_budget_bytes, coalesced into ragged batches of at most max_batch_rows
+   rows, and solved with `sweeps` FP64-residual corrections (more, up to
+   max_sweeps, while a batch misses its tightest tolerance) on up to
+   max_inflight concurrent streams.  The caller keeps a request's arrays
+   alive until tridi_server_wait returns for it. */
+tridi_status tridi_server_create(size_t hbm_budget_bytes, long max_batch_rows, int max_inflight, int sweeps,
+                                 int max_sweeps, void **server);
+size_t tridi_server_request_footprint(long rows, long num_systems);
+tridi_status tridi_server_submit(void *server, const float *a, const float *b, const float *c, const float *d,
+                                 double *x, const long *offsets, int num_systems, double tol, long long *id);
+/* Waits (timeout_ms < 0: forever) for request `id`; TRIDI_ERROR_BUSY on timeout.
+   *status is the request's own result (TRIDI_SUCCESS, TRIDI_ERROR_NOT_CONVERGED, ...). */
+tridi_status tridi_server_wait(void *server, long long id, int timeout_ms, int *status, int *sweeps,
+                               double *rel_residual, double *latency_us);
+tridi_status tridi_server_stats(void *server, long long *completed, long long *batches, long long *rows,
+                                double *max_inflight_seen);
+tridi_status tridi_server_destroy(void *server);
 
 /* Mixed-precision iterative refinement: FP32 a, b, c, d in, FP64 x out.
    Only the residual r = d - T x and the accumulation x += e run in FP64;

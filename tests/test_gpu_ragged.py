@@ -35,7 +35,8 @@ def _check_systems(a, b, c, d, x, off, idx, res_tol=RES_TOL[np.float32], fwd_tol
 def test_ragged_mixed_sizes(cuda, seed):
     rng = np.random.default_rng(seed)
     sizes = np.concatenate([rng.integers(1, 40, 50), rng.integers(40, 481, 300), rng.integers(481, 6000, 40),
-                            rng.integers(6000, 8705, 12), [1, 2, 3, 480, 481, 6141, 6144, 8704]])
+                            rng.integers(6000, 12281, 12),
+                            [1, 2, 3, 480, 481, 2400, 2401, 6141, 6144, 8704, 12279, 12280]])
     rng.shuffle(sizes)
     a, b, c, d, off = workloads.adi(sizes, seed=seed)
     total = int(off[-1])
@@ -74,14 +75,14 @@ def test_ragged_full_workload_100000_systems(cuda):
 
 
 def test_ragged_refined_graph_replay(cuda):
-    """Refinement of a ragged batch (systems up to 16384 rows, beyond shared
+    """Refinement of a ragged batch (systems up to 24480 rows, beyond shared
     memory) to 1e-10, captured once in a CUDA graph; replays agree bit for bit
     with the eager sequence and with the FP64 oracle."""
     from tridiagonalsolvers_gb300.ragged import RaggedRefiner
 
     rng = np.random.default_rng(3)
-    sizes = np.concatenate([rng.integers(32, 480, 200), rng.integers(480, 8704, 40), rng.integers(8705, 16385, 6),
-                            [16384, 17408]])
+    sizes = np.concatenate([rng.integers(32, 480, 200), rng.integers(480, 12280, 40), rng.integers(12281, 24481, 6),
+                            [16384, 24480]])
     a, b, c, d, off = workloads.adi(sizes, seed=5)
     total = int(off[-1])
     t = [_dev(cuda, v, total) for v in (a, b, c, d)]
@@ -104,8 +105,15 @@ def test_ragged_refined_graph_replay(cuda):
 
 
 def test_ragged_big_systems_plain(cuda):
-    sizes = np.array([8705, 12000, 16384, 17408, 100, 9000])
+    sizes = np.array([12281, 12000, 16384, 17408, 24480, 100, 9000, 20001])
     a, b, c, d, off = workloads.adi(sizes, seed=8)
     total = int(off[-1])
     x = RaggedPlan(off).solve(*(_dev(cuda, v, total) for v in (a, b, c, d))).cpu().numpy()[:total]
     _check_systems(a, b, c, d, x, off, range(len(sizes)))
+
+
+def test_ragged_rejects_oversize_systems():
+    from tridiagonalsolvers_gb300 import _lib
+
+    with pytest.raises(_lib.TridiError):
+        RaggedPlan(np.array([0, 100, 100 + 24481]))

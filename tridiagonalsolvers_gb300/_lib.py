@@ -64,6 +64,14 @@ _SIGS["tridi_ragged_refine_f32"] = (c_int, [_P, _P, _P, _P, _P, _P, _P, _P, c_in
 _SIGS["tridi_noalloc_max_unknowns"] = (ctypes.c_long, [])
 _SIGS["tridi_noalloc_last_cuda_error"] = (c_int, [])
 _SIGS["tridi_solve_interleaved_noalloc_f32"] = (c_int, [_P, _P, _P, _P, _P, ctypes.c_long, ctypes.c_long, _P])
+_LL = ctypes.c_longlong
+_SIGS["tridi_server_create"] = (c_int, [c_size_t, ctypes.c_long, c_int, c_int, c_int, POINTER(c_void_p)])
+_SIGS["tridi_server_request_footprint"] = (c_size_t, [ctypes.c_long, ctypes.c_long])
+_SIGS["tridi_server_submit"] = (c_int, [_P, _P, _P, _P, _P, _P, _P, c_int, c_double, POINTER(_LL)])
+_SIGS["tridi_server_wait"] = (c_int, [_P, _LL, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_double),
+                                      POINTER(c_double)])
+_SIGS["tridi_server_stats"] = (c_int, [_P, POINTER(_LL), POINTER(_LL), POINTER(_LL), POINTER(c_double)])
+_SIGS["tridi_server_destroy"] = (c_int, [_P])
 _SIGS["tridi_refine_workspace_bytes"] = (c_size_t, [ctypes.c_long, ctypes.c_long, c_int])
 _SIGS["tridi_refine_f32"] = (c_int, [_P, _P, _P, _P, _P, ctypes.c_long, ctypes.c_long, c_int, c_double, c_int, _P,
                                      c_size_t, _P, POINTER(c_int), POINTER(c_double)])

@@ -96,6 +96,74 @@ __device__ __forceinline__ void chunk_eliminate(Chunk<T, K>& ch, int k, bool fir
   }
 }
 
+// Summary of a chunk eliminated in shared memory: what the separator system
+// and the back substitution need besides the rows themselves.
+template <class T>
+struct ChunkSummary {
+  Row<T> sep;
+  T fD, fC, fA;
+  T lD, lC, lA;
+};
+
+// chunk_eliminate on rows held in shared memory (no size bound, K-free):
+// interior rows i < k-1 get (a, c, d) overwritten by (ap, cp, dp), so the
+// back substitution reads them again instead of holding 3k registers.
+template <class T>
+__device__ __forceinline__ void chunk_eliminate_smem(ChunkSummary<T>& cs, int k, bool first, bool last, T* sa,
+                                                     const T* sb, T* sc, T* sd) {
+  T cprev = T(0), aprev = T(0), dprev = T(0);
+#pragma unroll 4
+  for (int i = 0; i < k - 1; ++i) {
+    const T a = (i == 0 && first) ? T(0) : sa[i];
+    const T inv = tdiv(T(1), sb[i] - a * cprev);
+    const T cn = sc[i] * inv;
+    const T an = (i == 0 ? a : -a * aprev) * inv;
+    const T dn = (sd[i] - a * dprev) * inv;
+    sa[i] = an; sc[i] = cn; sd[i] = dn;
+    cprev = cn; aprev = an; dprev = dn;
+  }
+  T D = T(0), C = T(-1), A = T(0);
+#pragma unroll 4
+  for (int i = k - 2; i >= 0; --i) {
+    const T c = sc[i];
+    D = sd[i] - c * D;
+    C = -c * C;
+    A = sa[i] - c * A;
+  }
+  cs.fD = D; cs.fC = C; cs.fA = A;
+  if (k >= 2) {
+    cs.lD = dprev; cs.lC = cprev; cs.lA = aprev;
+  } else {
+    cs.lD = T(0); cs.lC = T(0); cs.lA = T(-1);
+  }
+  if (k >= 1) {
+    cs.sep = Row<T>{sa[k - 1], sb[k - 1], sc[k - 1], sd[k - 1]};
+    if (k == 1 && first) cs.sep.a = T(0);
+    if (last) cs.sep.c = T(0);
+  } else {
+    cs.sep = Row<T>{T(0), T(1), T(0), T(0)};
+  }
+}
+
+template <class T>
+__device__ __forceinline__ Row<T> separator_row_s(const ChunkSummary<T>& cs, T nD, T nC, T nA) {
+  const Row<T>& s = cs.sep;
+  return Row<T>{-s.a * cs.lA, s.b - s.a * cs.lC - s.c * nA, -s.c * nC, s.d - s.a * cs.lD - s.c * nD};
+}
+
+// Back substitution of a chunk eliminated by chunk_eliminate_smem; x_i
+// stored to dst[i] for i < k.
+template <class T>
+__device__ __forceinline__ void chunk_back_smem(int k, T sj, T sl, const T* sa, const T* sc, const T* sd, T* dst) {
+  if (k >= 1) dst[k - 1] = sj;
+  T xn = sj;
+#pragma unroll 4
+  for (int i = k - 2; i >= 0; --i) {
+    xn = sd[i] - sc[i] * xn - sa[i] * sl;
+    dst[i] = xn;
+  }
+}
+
 // The lane's row of the separator system, given the next chunk's first
 // interior row (nD, nC, nA).
 template <class T, int K>
@@ -132,6 +200,17 @@ __device__ __forceinline__ void chunk_back(const Chunk<T, K>& ch, int k, T sj, T
   }
 }
 
+// Same, storing each unknown to dst[i] (i < k) as soon as it is known.
+template <class T, int K>
+__device__ __forceinline__ void chunk_back_store(const Chunk<T, K>& ch, int k, T sj, T sl, T* dst) {
+  T xn = sj;
+#pragma unroll
+  for (int i = K - 1; i >= 0; --i) {
+    xn = (i <= k - 2) ? ch.dp[i] - ch.cp[i] * xn - ch.ap[i] * sl : sj;
+    if (i < k) dst[i] = xn;
+  }
+}
+
 // Whole system in one warp: lane l owns rows [l*kk, min(l*kk+kk, n)) of the
 // arrays (sa, sb, sc, sd).  Returns the lane's row count.
 template <class T, int K>
@@ -151,6 +230,25 @@ __device__ __forceinline__ int warp_partition_solve(int n, int kk, const T* sa, 
   if (lane == 0) sl = T(0);
   chunk_back<T, K>(ch, k, s, sl, x);
   return k;
+}
+
+// Same, each unknown stored to xg[lane * kk + i] as soon as it is known.
+template <class T, int K>
+__device__ __forceinline__ void warp_partition_solve_store(int n, int kk, const T* sa, const T* sb, const T* sc,
+                                                           const T* sd, T* xg) {
+  const int lane = threadIdx.x & 31;
+  const int r0 = lane * kk;
+  int k = n - r0;
+  k = k < 0 ? 0 : (k > kk ? kk : k);
+  Chunk<T, K> ch;
+  chunk_eliminate<T, K>(ch, k, lane == 0, r0 + k == n && k > 0, sa + r0, sb + r0, sc + r0, sd + r0);
+  const T nD = __shfl_down_sync(kFull, ch.fD, 1);
+  const T nC = __shfl_down_sync(kFull, ch.fC, 1);
+  const T nA = __shfl_down_sync(kFull, ch.fA, 1);
+  const T s = warp_pcr32<T>(separator_row<T, K>(ch, nD, nC, nA));
+  T sl = __shfl_up_sync(kFull, s, 1);
+  if (lane == 0) sl = T(0);
+  chunk_back_store<T, K>(ch, k, s, sl, xg + r0);
 }
 
 }  // namespace tridi
