@@ -424,13 +424,27 @@ def run_ragged(args):
 
     t = [up(v) for v in (a, b, c, d)]
     del a, b, c, d
+    # threads per system for each size bucket, timed on this GPU before the plan is built
+    from tridiagonalsolvers_gb300 import autotune
+
+    tuned = {}
+    if not args.no_autotune:
+        for k in autotune.DEFAULT_KEYS["ragged"]:
+            if k <= 8192:
+                tuned[str(k)] = autotune.tune("ragged", k)[0]
     plan = RaggedPlan(off, device=dev)
     x = torch.zeros(padded(total), dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
     ms = time_kernel(lambda: plan.solve(*t, x=x), stream, args.warmup, args.steps)
-    ref = RaggedRefiner(plan, *t, sweeps=args.sweeps, graph=True)
-    rms = time_kernel(ref.launch, stream, 2, max(2, args.steps // 2))
-    x64, rel = ref.run()
+    refined = {}
+    for mode in ("df", "fp64"):
+        ref = RaggedRefiner(plan, *t, sweeps=args.sweeps, graph=True, residual=mode)
+        rms = time_kernel(ref.launch, stream, 3, max(3, args.steps // 2))
+        _, rel = ref.run()
+        refined[mode] = {"value": total / (rms * 1e-3), "ms_per_step": rms, "sweeps": args.sweeps,
+                         "rel_residual": rel, "tol": 1e-10, "frac_of_plain": ms / rms, "cuda_graph": True,
+                         "residual_arithmetic": {"df": "double-float (FP32 pairs)", "fp64": "native FP64"}[mode]}
+        del ref
     peak, kind = measured_peaks()
     line = {
         "metric": METRIC, "value": total / (ms * 1e-3), "unit": "unknowns/s", "n_gpus": 1, "steps": args.steps,
@@ -438,15 +452,138 @@ def run_ragged(args):
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"ragged ADI batch, {count} systems, sizes log-uniform in [32, 8192]",
                    "total_unknowns": total, "work_items": plan.items, "seed": workloads.SEEDS["c4"],
-                   "l2": "inputs larger than L2"},
+                   "l2": "inputs larger than L2",
+                   "autotuned_threads_per_system": tuned or "built-in rule (--no-autotune)"},
         "roofline": {"bound": "hbm", "achieved": BYTES_PER_UNKNOWN * total / (ms * 1e-3) / 1e9, "peak": peak,
                      "unit": "GB/s", "frac": BYTES_PER_UNKNOWN * total / (ms * 1e-3) / 1e9 / peak,
                      "peak_source": kind, "traffic": None},
-        "refined": {"value": total / (rms * 1e-3), "ms_per_step": rms, "sweeps": args.sweeps, "rel_residual": rel,
-                    "tol": 1e-10, "frac_of_plain": ms / rms, "cuda_graph": True},
+        "refined": refined["df"],
+        "refined_fp64": refined["fp64"],
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_serve(args):
+    """Served request stream: requests of 1..4096 systems of 64..16384 unknowns
+    (log-uniform; diagonally dominant or ADI), host arrays in, FP64 x out,
+    refined to 1e-10 by the continuous-batching server.  First all requests
+    at once (saturation throughput), then Poisson arrivals at fractions of
+    that rate (p50 / p99 latency).  The plain FP32 form of the same rows on
+    the same GPU is timed beside it: device-resident (one ragged launch) and
+    end to end (pinned host buffers in and out)."""
+    import threading
+
+    import torch
+
+    from tridiagonalsolvers_gb300.ragged import RaggedPlan, padded
+    from tridiagonalsolvers_gb300.serve import Server, make_request
+
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(workloads_seed("c5"))
+    pool = [make_request(rng) for _ in range(args.serve_requests)]
+    rows = [int(r[4][-1]) for r in pool]
+    total = sum(rows)
+    srv = Server(hbm_budget_bytes=48 << 30, max_batch_rows=1 << 24, max_inflight=3, sweeps=args.sweeps,
+                 max_sweeps=args.sweeps + 2)
+
+    def serve_once(arrivals):
+        """Submits pool[i] at arrivals[i] seconds after the start; returns
+        (wall seconds, per-request info)."""
+        ids = [None] * len(pool)
+        t0 = time.perf_counter()
+        for i, (a, b, c, d, off) in enumerate(pool):
+            delay = arrivals[i] - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            ids[i] = srv.submit(a, b, c, d, off, tol=1e-10)
+        infos = [srv.wait(rid)[1] for rid in ids]
+        return time.perf_counter() - t0, infos
+
+    # warm up: kernels loaded, pools grown
+    for a, b, c, d, off in pool[:2]:
+        srv.wait(srv.submit(a, b, c, d, off))
+    wall, infos = serve_once([0.0] * len(pool))
+    sat = total / wall
+    def lat(infos):
+        v = np.array([i["latency_us"] for i in infos]) / 1e3
+        return {"p50_ms": float(np.percentile(v, 50)), "p99_ms": float(np.percentile(v, 99)),
+                "max_rel_residual": max(i["rel_residual"] for i in infos),
+                "sweeps_max": max(i["sweeps"] for i in infos)}
+    sweep = [{"offered_frac_of_saturation": 1.0, "arrivals": "all at t=0", "unknowns_per_s": sat, **lat(infos)}]
+    req_rate = len(pool) / wall
+    arng = np.random.default_rng(workloads_seed("c5") + 1)
+    for frac in (0.5, 0.8):
+        gaps = arng.exponential(1.0 / (frac * req_rate), len(pool))
+        arr = np.concatenate([[0.0], np.cumsum(gaps[:-1])])
+        w, inf = serve_once(arr)
+        sweep.append({"offered_frac_of_saturation": frac, "arrivals": "poisson", "rate_req_per_s": frac * req_rate,
+                      "unknowns_per_s": total / w, **lat(inf)})
+    stats = srv.stats()
+    srv.close()
+
+    # plain FP32 form of the same rows on the same GPU
+    off_all = np.concatenate([[0], np.cumsum(rows)]).astype(np.int64)
+    sys_off = [0]
+    for r in pool:
+        o = r[4]
+        sys_off.extend((o[1:] + sys_off[-1]).tolist())
+    sys_off = np.array(sys_off, dtype=np.int64)
+    cat = [np.concatenate([r[q] for r in pool]) for q in range(4)]
+    need = padded(total)
+    host = []
+    for v in cat:
+        h = torch.zeros(need, dtype=torch.float32).pin_memory()
+        h[:total] = torch.from_numpy(v)
+        host.append(h)
+    hx = torch.zeros(need, dtype=torch.float32).pin_memory()
+    dv = [torch.empty(need, dtype=torch.float32, device=dev) for _ in range(4)]
+    dx = torch.empty(need, dtype=torch.float32, device=dev)
+    for h, t in zip(host, dv):
+        t.copy_(h)
+    plan = RaggedPlan(sys_off, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ms_dev = time_kernel(lambda: plan.solve(*dv, x=dx), stream, 3, 10)
+
+    def e2e():
+        for h, t in zip(host, dv):
+            t.copy_(h, non_blocking=True)
+        plan.solve(*dv, x=dx)
+        hx.copy_(dx, non_blocking=True)
+        torch.cuda.synchronize()
+
+    e2e()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        e2e()
+    e2e_s = (time.perf_counter() - t0) / 5
+    plain_dev = total / (ms_dev * 1e-3)
+    plain_e2e = total / e2e_s
+    del off_all
+    line = {
+        "metric": METRIC, "value": sat, "unit": "unknowns/s", "n_gpus": 1, "steps": len(pool), "warmup": 2,
+        "ms_per_step": wall / len(pool) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 solves, double-float residual, f64 x", "data": "synthetic",
+        "config": {"workload": f"served request stream, {len(pool)} requests of 1-4096 systems x 64-16384 unknowns "
+                               "(log-uniform, dominant or ADI), refined to 1e-10",
+                   "total_unknowns": total, "seed": workloads_seed("c5"), "sweeps": args.sweeps,
+                   "server": {"hbm_budget_gb": 48, "max_batch_rows": 1 << 24, "max_inflight": 3}},
+        "e2e": {"value": sat, "unit": "unknowns/s", "h2d_bytes_per_step": 16 * total / len(pool),
+                "d2h_bytes_per_step": 8 * total / len(pool), "path": "tridi_server_submit / tridi_server_wait"},
+        "latency_sweep": sweep,
+        "server_stats": stats,
+        "plain_fp32_same_rows": {"device_resident_unknowns_per_s": plain_dev, "e2e_unknowns_per_s": plain_e2e,
+                                 "served_frac_of_plain_e2e": sat / plain_e2e,
+                                 "served_frac_of_plain_device": sat / plain_dev},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workloads_seed(tag):
+    from tridiagonalsolvers_gb300 import workloads
+
+    return workloads.SEEDS[tag]
 
 
 def main():
@@ -457,11 +594,13 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-table", action="store_true", help="skip the per-kernel table")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--workload", default="batch", choices=["batch", "large", "ragged"],
+    ap.add_argument("--workload", default="batch", choices=["batch", "large", "ragged", "serve"],
                     help="batch: 65536 x 256 (default, the headline); large: 1024 x 65536 interleaved; "
-                         "ragged: 100000 ADI systems of 32..8192 unknowns")
+                         "ragged: 100000 ADI systems of 32..8192 unknowns; serve: a served request stream")
     ap.add_argument("--ragged-count", type=int, default=100000, help="systems of the ragged workload")
-    ap.add_argument("--sweeps", type=int, default=1, help="refinement sweeps of the ragged workload")
+    ap.add_argument("--sweeps", type=int, default=1, help="refinement sweeps of the ragged / serve workloads")
+    ap.add_argument("--serve-requests", type=int, default=200, help="requests of the serve workload")
+    ap.add_argument("--no-autotune", action="store_true", help="ragged workload: keep the built-in size classes")
     ap.add_argument("--large-n", type=int, default=65536, help="system size of the large workload")
     ap.add_argument("--no-refine", action="store_true", help="large workload: plain solve only")
     args = ap.parse_args()
@@ -473,6 +612,8 @@ def main():
         return run_large(args)
     if args.workload == "ragged":
         return run_ragged(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_gpu(args)
 
 

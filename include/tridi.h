@@ -66,6 +66,9 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
 #define TRIDI_TUNE_STAGES 1     /* cp.async.bulk pipeline stages per CTA (1..8) */
 #define TRIDI_TUNE_CRPCR_REST 2 /* switch level of the CR-PCR correction solves */
 #define TRIDI_TUNE_CR_ROWS 3    /* rows per thread of the CR/PCR/CR-PCR kernels (2, 4, 8, 16) */
+#define TRIDI_TUNE_RESIDUAL 4   /* arithmetic of the fused ragged refinement's residual and update: */
+#define TRIDI_RESIDUAL_DF 1     /*   double-float (pairs of FP32, 48-bit significand; the default) */
+#define TRIDI_RESIDUAL_FP64 2   /*   native FP64 */
 tridi_status tridi_set_tunable(int key, int value);
 int tridi_get_tunable(int key);
 
@@ -113,7 +116,8 @@ tridi_status tridi_crpcr_nbc_f64(const double *a, const double *b, const double 
    pcrGauss_kernel.cu:1-126).  `gaussian` = g, the number of interleaved
    subsystems (a power of two, 1 <= g <= n) solved by Thomas after log2(g) PCR
    steps.  Exact for every g (the reference's step table is exact only when
-   g = 2^it).  Any 1 <= n <= 4096. */
+   g = 2^it).  gaussian = 0: the autotuned g for n (TRIDI_AUTOTUNE_PCR_THOMAS_SPLIT),
+   else one chain per thread of the system.  Any 1 <= n <= 4096. */
 tridi_status tridi_pcr_thomas_f32(const float *a, const float *b, const float *c, const float *d, float *x, int n,
                                   int num_systems, int gaussian, tridi_stream_t stream);
 tridi_status tridi_pcr_thomas_f64(const double *a, const double *b, const double *c, const double *d, double *x,
@@ -145,6 +149,32 @@ tridi_status tridi_solve_large_f64(const double *a, const double *b, const doubl
                                    long n, long num_systems, int layout, void *workspace, size_t workspace_bytes,
                                    tridi_stream_t stream);
 
+/* Autotuner (GB300 addition).  Times the candidates of one tuning decision on
+   a seeded synthetic batch of about sample_unknowns unknowns (<= 0: 2^24) on
+   `stream`, records the fastest in the process-wide table and returns it in
+   *chosen (and its time per launch in *best_ms; either may be NULL):
+     TRIDI_AUTOTUNE_CRPCR_REST    key n (power of two, 4..4096): the CR-to-PCR
+        switch level (rest system size, 2..n/2) that the refinement's FP32
+        correction solves use; diagonally dominant systems.
+     TRIDI_AUTOTUNE_PCR_THOMAS_SPLIT  key n (power of two, 2..4096): the number
+        of Thomas chains g (PCR steps = log2 g) that tridi_pcr_thomas_* use
+        when called with gaussian = 0; diagonally dominant systems.
+     TRIDI_AUTOTUNE_RAGGED_THREADS    key: any size in the bucket
+        [2^k, 2^(k+1)), k = 0..14: threads per system (32, 160 or 480) that
+        ragged plans created afterwards give systems of that bucket; ADI
+        systems.
+   tridi_tuned / tridi_set_tuned read and write the table (key as above,
+   0 = not tuned: the built-in choice applies), tridi_autotune_reset clears
+   it.  Synchronises `stream`; allocates and frees its own sample. */
+#define TRIDI_AUTOTUNE_CRPCR_REST 0
+#define TRIDI_AUTOTUNE_PCR_THOMAS_SPLIT 1
+#define TRIDI_AUTOTUNE_RAGGED_THREADS 2
+tridi_status tridi_autotune(int table, long key, long sample_unknowns, tridi_stream_t stream, int *chosen,
+                            float *best_ms);
+int tridi_tuned(int table, long key);
+tridi_status tridi_set_tuned(int table, long key, int value);
+tridi_status tridi_autotune_reset(void);
+
 /* Ragged batches (GB300 addition): systems of different sizes, concatenated --
    system s owns rows [offsets[s], offsets[s+1]) -- solved by one persistent
    launch driven by a size-bucketed work queue.  Sizes 1 .. 24480.  The plan is
@@ -162,11 +192,13 @@ tridi_status tridi_ragged_plan_upload(const void *plan, void *dev_plan, size_t d
 tridi_status tridi_ragged_plan_destroy(void *plan);
 tridi_status tridi_ragged_solve_f32(const float *a, const float *b, const float *c, const float *d, float *x,
                                     const void *plan, void *dev_plan, tridi_stream_t stream);
-/* Ragged FP32 solves with FP64 residual and FP64 accumulation, a fixed number
-   of correction sweeps and no host synchronisation (capturable in a CUDA
-   graph).  x: FP64, round_up(total_rows, 4) elements.  offsets_dev: the
-   plan's offsets in device memory.  *dev_rel (device) receives the final
-   maximum relative residual ||d - T x|| / ||d||. */
+/* Fused mixed-precision refinement of a ragged batch in one launch: per
+   system, an FP32 solve, then `sweeps` times { r = d - T x and x += e in
+   extended precision (TRIDI_TUNE_RESIDUAL), FP32 solve of T e = r }, all
+   inside the SM; x written once in FP64 (round_up(total_rows, 4) elements).
+   *dev_rel (device) receives the maximum over systems of ||d - T x||_2 /
+   ||d||_2.  No host synchronisation (capturable in a CUDA graph).
+   offsets_dev may be NULL. */
 size_t tridi_ragged_refine_workspace_bytes(long total_rows, long num_systems);
 tridi_status tridi_ragged_refine_f32(const float *a, const float *b, const float *c, const float *d, double *x,
                                      const void *plan, void *dev_plan, const long *offsets_dev, int sweeps,

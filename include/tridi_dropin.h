@@ -84,6 +84,15 @@ tridi_status tridi_dropin_solve_f64(int algo, const double *a, const double *b, 
 /* Frees the persistent drop-in workspace of the current device. */
 tridi_status tridi_dropin_release(void);
 
+/* Text dump of a host solution in the reference driver's format
+   (writeResultToFile, tridiagonal_gold.h:96-107; written by
+   test_tridiagonal.cpp:103-104 as cpu_result.txt / gpu_result.txt): per
+   system a line "***The following is the result of the equation set <s>",
+   then one value per line in the C++ stream's default format (6 significant
+   digits), so dumps of both builds diff line by line. */
+tridi_status tridi_write_result_file_f32(const float *x, int num_systems, int system_size, const char *path);
+tridi_status tridi_write_result_file_f64(const double *x, int num_systems, int system_size, const char *path);
+
 #ifdef __cplusplus
 }
 #endif

@@ -50,6 +50,8 @@ for _prec in ("f32", "f64"):
     _SIGS[f"tridi_solve_large_{_prec}"] = (c_int, [_P, _P, _P, _P, _P, ctypes.c_long, ctypes.c_long, c_int, _P,
                                                    c_size_t, _P])
 _SIGS["tridi_dropin_release"] = (c_int, [])
+_SIGS["tridi_write_result_file_f32"] = (c_int, [_P, c_int, c_int, c_char_p])
+_SIGS["tridi_write_result_file_f64"] = (c_int, [_P, c_int, c_int, c_char_p])
 _SIGS["tridi_large_workspace_bytes"] = (c_size_t, [ctypes.c_long, ctypes.c_long, c_int])
 _SIGS["tridi_ragged_plan_create"] = (c_int, [_P, c_int, POINTER(c_void_p)])
 _SIGS["tridi_ragged_plan_device_bytes"] = (c_size_t, [_P])
@@ -65,6 +67,11 @@ _SIGS["tridi_noalloc_max_unknowns"] = (ctypes.c_long, [])
 _SIGS["tridi_noalloc_last_cuda_error"] = (c_int, [])
 _SIGS["tridi_solve_interleaved_noalloc_f32"] = (c_int, [_P, _P, _P, _P, _P, ctypes.c_long, ctypes.c_long, _P])
 _LL = ctypes.c_longlong
+_SIGS["tridi_autotune"] = (c_int, [c_int, ctypes.c_long, ctypes.c_long, _P, POINTER(c_int),
+                                   POINTER(ctypes.c_float)])
+_SIGS["tridi_tuned"] = (c_int, [c_int, ctypes.c_long])
+_SIGS["tridi_set_tuned"] = (c_int, [c_int, ctypes.c_long, c_int])
+_SIGS["tridi_autotune_reset"] = (c_int, [])
 _SIGS["tridi_server_create"] = (c_int, [c_size_t, ctypes.c_long, c_int, c_int, c_int, POINTER(c_void_p)])
 _SIGS["tridi_server_request_footprint"] = (c_size_t, [ctypes.c_long, ctypes.c_long])
 _SIGS["tridi_server_submit"] = (c_int, [_P, _P, _P, _P, _P, _P, _P, c_int, c_double, POINTER(_LL)])

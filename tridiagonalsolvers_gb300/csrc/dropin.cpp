@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <mutex>
 
 #include "runtime.h"
@@ -205,6 +206,34 @@ tridi_status tridi_dropin_solve_f64(int algo, const double* a, const double* b, 
                                     double* x, int n, int m, int param) {
   return tridi::host_solve<double>(algo, a, b, c, d, x, n, m, param);
 }
+}  // extern "C"
+
+namespace tridi {
+namespace {
+template <class T>
+tridi_status write_result(const T* x, int m, int n, const char* path) {
+  if (!x || !path || m < 0 || n < 0) return TRIDI_ERROR_INVALID_VALUE;
+  std::ofstream f(path);
+  if (!f) return TRIDI_ERROR_INVALID_VALUE;
+  const long total = (long)m * n;
+  for (long i = 0; i < total; ++i) {
+    if (i % n == 0) f << "***The following is the result of the equation set " << i / n << "\n";
+    f << x[i] << "\n";
+  }
+  return f ? TRIDI_SUCCESS : TRIDI_ERROR_INVALID_VALUE;
+}
+}  // namespace
+}  // namespace tridi
+
+extern "C" {
+
+tridi_status tridi_write_result_file_f32(const float* x, int m, int n, const char* path) {
+  return tridi::write_result(x, m, n, path);
+}
+tridi_status tridi_write_result_file_f64(const double* x, int m, int n, const char* path) {
+  return tridi::write_result(x, m, n, path);
+}
+
 tridi_status tridi_dropin_release(void) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

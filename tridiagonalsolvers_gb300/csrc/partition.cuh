@@ -151,16 +151,17 @@ __device__ __forceinline__ Row<T> separator_row_s(const ChunkSummary<T>& cs, T n
   return Row<T>{-s.a * cs.lA, s.b - s.a * cs.lC - s.c * nA, -s.c * nC, s.d - s.a * cs.lD - s.c * nD};
 }
 
-// Back substitution of a chunk eliminated by chunk_eliminate_smem; x_i
-// stored to dst[i] for i < k.
-template <class T>
-__device__ __forceinline__ void chunk_back_smem(int k, T sj, T sl, const T* sa, const T* sc, const T* sd, T* dst) {
-  if (k >= 1) dst[k - 1] = sj;
+// Back substitution of a chunk eliminated by chunk_eliminate_smem: emit(i, x_i)
+// for every row i < k of the chunk, last row first.
+template <class T, class Emit>
+__device__ __forceinline__ void chunk_back_smem(int k, T sj, T sl, const T* sa, const T* sc, const T* sd,
+                                                Emit& emit) {
+  if (k >= 1) emit(k - 1, sj);
   T xn = sj;
 #pragma unroll 4
   for (int i = k - 2; i >= 0; --i) {
     xn = sd[i] - sc[i] * xn - sa[i] * sl;
-    dst[i] = xn;
+    emit(i, xn);
   }
 }
 
@@ -200,14 +201,14 @@ __device__ __forceinline__ void chunk_back(const Chunk<T, K>& ch, int k, T sj, T
   }
 }
 
-// Same, storing each unknown to dst[i] (i < k) as soon as it is known.
-template <class T, int K>
-__device__ __forceinline__ void chunk_back_store(const Chunk<T, K>& ch, int k, T sj, T sl, T* dst) {
+// Same, handing each unknown to emit(i, x_i) (i < k) as soon as it is known.
+template <class T, int K, class Emit>
+__device__ __forceinline__ void chunk_back_emit(const Chunk<T, K>& ch, int k, T sj, T sl, Emit& emit) {
   T xn = sj;
 #pragma unroll
   for (int i = K - 1; i >= 0; --i) {
     xn = (i <= k - 2) ? ch.dp[i] - ch.cp[i] * xn - ch.ap[i] * sl : sj;
-    if (i < k) dst[i] = xn;
+    if (i < k) emit(i, xn);
   }
 }
 
@@ -230,25 +231,6 @@ __device__ __forceinline__ int warp_partition_solve(int n, int kk, const T* sa, 
   if (lane == 0) sl = T(0);
   chunk_back<T, K>(ch, k, s, sl, x);
   return k;
-}
-
-// Same, each unknown stored to xg[lane * kk + i] as soon as it is known.
-template <class T, int K>
-__device__ __forceinline__ void warp_partition_solve_store(int n, int kk, const T* sa, const T* sb, const T* sc,
-                                                           const T* sd, T* xg) {
-  const int lane = threadIdx.x & 31;
-  const int r0 = lane * kk;
-  int k = n - r0;
-  k = k < 0 ? 0 : (k > kk ? kk : k);
-  Chunk<T, K> ch;
-  chunk_eliminate<T, K>(ch, k, lane == 0, r0 + k == n && k > 0, sa + r0, sb + r0, sc + r0, sd + r0);
-  const T nD = __shfl_down_sync(kFull, ch.fD, 1);
-  const T nC = __shfl_down_sync(kFull, ch.fC, 1);
-  const T nA = __shfl_down_sync(kFull, ch.fA, 1);
-  const T s = warp_pcr32<T>(separator_row<T, K>(ch, nD, nC, nA));
-  T sl = __shfl_up_sync(kFull, s, 1);
-  if (lane == 0) sl = T(0);
-  chunk_back_store<T, K>(ch, k, s, sl, xg + r0);
 }
 
 }  // namespace tridi

@@ -184,7 +184,19 @@ tridi_status pcr_thomas_device(const T* a, const T* b, const T* c, const T* d, T
                                tridi_stream_t stream) {
   if (!a || !b || !c || !d || !x || m <= 0) return TRIDI_ERROR_INVALID_VALUE;
   const int nmax = 4096;
-  if (n < 1 || n > nmax || !is_pow2(g) || g > n) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  if (n < 1 || n > nmax || g < 0) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  if (g == 0) {  // the autotuned split for this n, else one chain per thread of the system
+    const int t = is_pow2(n) ? tuned(TRIDI_AUTOTUNE_PCR_THOMAS_SPLIT, ilog2(n)) : 0;
+    if (t > 0 && is_pow2(t) && t <= n) {
+      g = t;
+    } else {
+      int tp = 32;
+      while (tp < 256 && tp < n) tp *= 2;
+      g = 1;
+      while (2 * g <= n && 2 * g <= tp) g *= 2;
+    }
+  }
+  if (!is_pow2(g) || g > n) return TRIDI_ERROR_UNSUPPORTED_SIZE;
   const DeviceInfo* dev = current_device();
   if (!dev) return TRIDI_ERROR_CUDA;
   PTParams p{};

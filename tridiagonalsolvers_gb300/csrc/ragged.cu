@@ -7,8 +7,7 @@
 //   MULTI  up to 15 systems of <= 480 rows: one warp per system
 //   MULTI4 up to 3 systems of 481 .. 2400 rows: 160 threads (own named
 //          barrier) per system, three systems at once
-//   SINGLE one system of 2401 .. ~6140 rows: the whole CTA
-//   DOUBLE one system of up to 12280 rows: the whole CTA, both stage buffers
+//   SINGLE one system of 2401 .. ~13800 rows: the whole CTA
 //   BIG    one system of up to 24480 rows, read from global memory (no
 //          staging): every thread owns three chunks of up to 17 rows; pass 1
 //          eliminates them and exports their interfaces, the 1440
@@ -17,15 +16,35 @@
 // One CTA per SM (480 consumer threads + a producer warp).  Items are sorted
 // largest first and CTA b takes items b, b + grid, b + 2 grid, ... (so every
 // CTA gets the same mix of sizes, and no claim has to wait on an atomic).
-// Its producer stages each item into one of two shared-memory buffers with
-// cp.async.bulk (each system's 16-byte-aligned row range, per array) while
-// the consumers solve the previous one, and publishes the item through the
-// stage's mbarrier; a DOUBLE waits for both buffers.
+//
+// Staging.  Shared memory holds a ring of rows (a, b, c, d, and in the
+// refined modes the two words of x): the producer places each item's rows
+// contiguously at the ring's head (wrapping to row 0 when the tail end is too
+// short), copies every system's 16-byte-aligned row range per array with
+// cp.async.bulk, and publishes the item in one of kSlots descriptor slots
+// through that slot's mbarrier.  Consumers take items in order and release
+// each slot when done; the producer reclaims ring rows oldest first.  So up
+// to kSlots items of any size are in flight, and a large item's copy overlaps
+// the solve of the items before it.
+//
 // Arithmetic: the partition solver of partition.cuh, per warp (MULTI), per
-// group of 160 threads (MULTI4) or per CTA (SINGLE / DOUBLE), with the chunk
-// elimination done in place in the stage buffer (no register arrays, so no
-// bound on rows per thread) and the separators solved by PCR in shuffles
-// (warp) or shared memory (group, CTA).
+// group of 160 threads (MULTI4) or per CTA (SINGLE), with the chunk
+// elimination done in place in the ring (no register arrays, so no bound on
+// rows per thread) and the separators solved by PCR in shuffles (warp) or
+// shared memory (group, CTA).
+//
+// Refined modes (tridi_ragged_refine_f32): every system is refined where it
+// sits, without leaving the SM: FP32 solve -> x; then `sweeps` times
+// { r = d - T x (extended precision; the original a, c, d are re-read from
+// L2 by the same loop and put back into the ring, where the FP32 elimination
+// had overwritten them); FP32 solve of T e = r in the ring; x += e (extended
+// precision) }; finally ||d - T x|| / ||d|| per system (its maximum over the
+// batch goes to one device word) and x is written once as FP64.  So HBM sees
+// each coefficient once and each unknown once (16 B in, 8 B out per row).
+// Extended precision is either native FP64 (RES_FP64) or double-float, an
+// unevaluated sum of two FP32 values with a 48-bit significand (RES_DF).
+// BIG systems refine the same way with their x and r in a global scratch.
+//
 // The arrays must hold at least round_up(total_rows, 4) elements and be
 // 16-byte aligned (the bulk copies read whole 16-byte groups).
 #include <algorithm>
@@ -40,26 +59,44 @@ namespace tridi {
 constexpr int kRagThreads = 480;       // consumer threads per CTA (15 warps; + 1 producer warp = 16 warps,
                                        // 4 per SM sub-partition, so up to 128 registers per thread)
 constexpr int kRagWarps = kRagThreads / 32;
-constexpr int kStageRows = 6144;       // rows per stage buffer (per array)
+constexpr int kSlots = 4;              // items in flight (descriptor slots)
 constexpr int kWarpMaxRows = 480;      // MULTI systems: up to 15 rows per lane
-constexpr int kMaxItemSystems = kRagWarps;       // 15
-constexpr int kMaxSystemRows = 2 * kStageRows - 8;  // 12280: largest staged system (a DOUBLE item)
-constexpr int kBigChunks = 3;                      // chunks per thread for BIG systems
-constexpr int kBigSepRows = kBigChunks * kRagThreads;      // chunks (separators) of a BIG system
-constexpr int kMaxBigRows = 17 * kBigSepRows;              // 24480
+constexpr int kGroup4Threads = 160;    // MULTI4: threads per system (5 warps)
+constexpr int kGroup4MaxRows = 2400;   // MULTI4 systems: up to 15 rows per thread
+constexpr int kMaxItemSystems = kRagWarps;  // 15
+constexpr int kBigChunks = 3;                           // chunks per thread for BIG systems
+constexpr int kBigSepRows = kBigChunks * kRagThreads;   // chunks (separators) of a BIG system
+constexpr int kBigKC = 17;                              // rows per BIG chunk at most
+constexpr int kMaxBigRows = kBigKC * kBigSepRows;       // 24480
+constexpr int kBigScratchRows = 2 * kBigSepRows;        // ring rows a BIG item borrows as scratch
 
-enum ItemKind : int { kMulti = 0, kSingle = 1, kDouble = 2, kNop = 3, kCont = 4, kEnd = 5, kBig = 6, kMulti4 = 7 };
-constexpr int kGroup4Threads = 160;                    // MULTI4: threads per system (5 warps)
-constexpr int kGroup4MaxRows = 2400;                   // MULTI4 systems: up to 15 rows per thread
+enum ItemKind : int { kMulti = 0, kMulti4 = 1, kSingle = 2, kBig = 3, kEnd = 4 };
+enum RagMode : int { kPlain = 0, kRefineDF = 1, kRefineFP64 = 2 };
+
+// Shared-memory map: [head: 2 x kSlots mbarriers, kSlots descriptors]
+// [group scratch: kGroupFloats] [ring: ring_arrays(M) x ring_rows(M) floats].
+constexpr int kHeadBytes = 1280;
+constexpr int kGroupFloats = 4 * kRagThreads + kRagThreads + 48 + 2 * 2 * kRagWarps;  // R, X, F0, norms
+constexpr int kSmemBudget = 232448;  // 227 KB, the opt-in maximum of sm_100-class GPUs
+__host__ __device__ constexpr int ring_arrays(int mode) { return mode == kPlain ? 4 : 6; }
+__host__ __device__ constexpr int ring_rows(int mode) {
+  return ((kSmemBudget - kHeadBytes - 4 * kGroupFloats) / (4 * ring_arrays(mode))) & ~255;
+}
+constexpr size_t rag_smem_bytes(int mode) {
+  return (size_t)kHeadBytes + 4 * (size_t)kGroupFloats + 4 * (size_t)ring_arrays(mode) * ring_rows(mode);
+}
+static_assert(ring_rows(kPlain) >= 13568 && ring_rows(kRefineDF) >= 8960, "ring sizes");
+static_assert(kBigScratchRows <= ring_rows(kRefineDF), "BIG scratch fits the ring");
+constexpr int kMaxStagedRows = ring_rows(kPlain);
 
 struct RagItem {
   int kind;
-  int count;        // systems in the item
-  int first;        // index into the plan's system list
-  int rows;         // padded rows the item occupies in the stage (per array)
+  int count;  // systems in the item
+  int first;  // index into the plan's system list
+  int rows;   // ring rows the item occupies (padded, per array)
 };
 
-// Plan buffer on the device: [counter (16 B)] [items] [system list].
+// Plan buffer on the device: [reserved (64 B)] [items] [system list].
 struct RagSys {
   long off;  // first row of the system
   int n;     // rows
@@ -71,19 +108,29 @@ struct RagParams {
   const float* b;
   const float* c;
   const float* d;
-  float* x;
+  float* x;                  // plain mode: FP32 solution
+  double* x64;               // refined modes: FP64 solution
+  float* wxh;                // refined modes, BIG systems: x (two words per row) and r, per row
+  float* wxl;
+  float* wr;
+  unsigned long long* rel;   // refined modes: max relative residual (bits of a non-negative double)
   const RagItem* items;
   const RagSys* sys;
   int nitems;
-  unsigned* counter;
+  int sweeps;
   unsigned* status;
 };
 
-struct RagStage {  // per-stage descriptor published by the producer
-  int item;        // index into items, or -1 for NOP / CONT / END markers
+struct RagSlot {  // descriptor of an item in flight, written by the producer warp
+  long off[kMaxItemSystems];  // first row of each system in the batch
+  int n[kMaxItemSystems];     // rows of each system
+  int base[kMaxItemSystems];  // ring row of each system's first row
   int kind;
-  int base[kMaxItemSystems];  // row of each system's first row inside the stage
+  int count;  // systems in the item
+  int rbase;  // first ring row of the item
+  int rrows;  // ring rows it holds
 };
+static_assert(2 * kSlots * 8 + kSlots * sizeof(RagSlot) <= kHeadBytes, "head fits");
 
 __device__ __forceinline__ int odd_ceil_dev(int v) { return (v & 1) ? v : v + 1; }
 
@@ -92,14 +139,154 @@ __device__ __forceinline__ int odd_ceil_dev(int v) { return (v & 1) ? v : v + 1;
 __device__ __forceinline__ void group_sync(int id, int count) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
+// Barrier of a solve group: the warp itself (gt == 32) or its named barrier.
+__device__ __forceinline__ void gsync(int bar, int gt) {
+  if (gt == 32)
+    __syncwarp();
+  else
+    group_sync(bar, gt);
+}
 
-// One system of n rows (shared-memory arrays sa..sd, overwritten) solved by a
-// group of gt threads (thread gtid of the group; gt == 32: one warp, else a
-// named barrier `bar` over the group): chunk elimination in place, the gt
+// ---------------------------------------------------------------------------
+// Extended-precision helpers of the refined modes.
+
+// Exact float -> double by assembling the IEEE-754 fields (normal numbers and
+// zeros; subnormals, infinities and NaNs take the conversion instruction).
+// Keeps the residual's conversions off the FP64 pipe.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e - 1u < 254u) {
+    const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+  }
+  if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+  return (double)f;
+}
+
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return s;
+}
+// Dekker's FastTwoSum (|a| >= |b| or a == 0).
+__device__ __forceinline__ float fast_two_sum(float a, float b, float& e) {
+  const float s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+  return s;
+}
+
+// x_i of the refined modes lives in two float words per row:
+//   RES_DF:   (hi, lo), x = hi + lo, |lo| <= ulp(hi) / 2
+//   RES_FP64: the low and high 32 bits of the double
+template <int MODE>
+struct XStore {
+  float* h;
+  float* l;
+  __device__ __forceinline__ double get64(int i) const {
+    if constexpr (MODE == kRefineFP64)
+      return __hiloint2double(__float_as_int(l[i]), __float_as_int(h[i]));
+    else
+      return f2d_exact(h[i]) + f2d_exact(l[i]);
+  }
+  __device__ __forceinline__ void set64(int i, double v) {
+    h[i] = __int_as_float(__double2loint(v));
+    l[i] = __int_as_float(__double2hiint(v));
+  }
+  // x_i = v (first solve)
+  __device__ __forceinline__ void init(int i, float v) {
+    if constexpr (MODE == kRefineFP64) {
+      set64(i, f2d_exact(v));
+    } else {
+      h[i] = v;
+      l[i] = 0.f;
+    }
+  }
+  // x_i += v (correction)
+  __device__ __forceinline__ void add(int i, float v) {
+    if constexpr (MODE == kRefineFP64) {
+      set64(i, get64(i) + f2d_exact(v));
+    } else {
+      float e;
+      const float s = two_sum(h[i], v, e);
+      float lo;
+      h[i] = fast_two_sum(s, __fadd_rn(e, l[i]), lo);
+      l[i] = lo;
+    }
+  }
+  // r_i = d - a x_{i-1} - b x_i - c x_{i+1}, rounded to float (a = 0 at
+  // i = 0, c = 0 at i = n - 1, as in the gold solver).
+  __device__ __forceinline__ float residual(int i, int n, float a, float b, float c, float d) const {
+    if constexpr (MODE == kRefineFP64) {
+      double r = fma(-f2d_exact(b), get64(i), f2d_exact(d));
+      if (i > 0) r = fma(-f2d_exact(a), get64(i - 1), r);
+      if (i < n - 1) r = fma(-f2d_exact(c), get64(i + 1), r);
+      return (float)r;
+    } else {
+      // products of the high words exactly (TwoProd), summed with TwoSum;
+      // the low words' products and all rounding errors go to t
+      const float hm = i > 0 ? h[i - 1] : 0.f, lm = i > 0 ? l[i - 1] : 0.f;
+      const float hp = i < n - 1 ? h[i + 1] : 0.f, lp = i < n - 1 ? l[i + 1] : 0.f;
+      const float am = i > 0 ? a : 0.f, cp = i < n - 1 ? c : 0.f;
+      const float h0 = h[i], l0 = l[i];
+      const float pb = __fmul_rn(b, h0), pa = __fmul_rn(am, hm), pc = __fmul_rn(cp, hp);
+      float t = -(fmaf(b, h0, -pb) + fmaf(am, hm, -pa) + fmaf(cp, hp, -pc));
+      float e;
+      float s = two_sum(d, -pb, e);
+      t += e;
+      s = two_sum(s, -pa, e);
+      t += e;
+      s = two_sum(s, -pc, e);
+      t += e;
+      t = fmaf(-b, l0, t);
+      t = fmaf(-am, lm, t);
+      t = fmaf(-cp, lp, t);
+      return __fadd_rn(s, t);
+    }
+  }
+};
+
+// Adds (rr, dd) over a solve group, and its leader folds sqrt(rr) / sqrt(dd)
+// into the batch maximum.  red: 2 doubles per warp of the CTA.
+__device__ __forceinline__ void group_rel_max(float rr, float dd, int gt, int bar, int gtid, double* red,
+                                              unsigned long long* rel) {
+  double r2 = rr, d2 = dd;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    r2 += __shfl_down_sync(kFull, r2, o);
+    d2 += __shfl_down_sync(kFull, d2, o);
+  }
+  if (gt > 32) {
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+      red[2 * w] = r2;
+      red[2 * w + 1] = d2;
+    }
+    group_sync(bar, gt);
+    if (gtid == 0) {
+      for (int q = 1; q < gt / 32; ++q) {
+        r2 += red[2 * (w + q)];
+        d2 += red[2 * (w + q) + 1];
+      }
+    }
+  }
+  if (gtid == 0) {
+    const double v = d2 > 0.0 ? sqrt(r2) / sqrt(d2) : sqrt(r2);
+    atomicMax(rel, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// One system of n rows (ring arrays sa..sd, overwritten) solved by a group of
+// gt threads (thread gtid of the group; gt == 32: one warp, else the named
+// barrier `bar` over the group): chunk elimination in place, the gt
 // separators solved by PCR (warp shuffles, or shared memory R: 4*gt floats,
-// X: gt, F0: 3*(gt/32)), back substitution; x written to global memory.
+// X: gt, F0: 3*(gt/32)), back substitution; emit(i, x_i) for every row.
+template <class Emit>
 __device__ __forceinline__ void group_solve(int n, int gt, int bar, int gtid, float* sa, const float* sb, float* sc,
-                                            float* sd, float* R, float* X, float* F0, float* xg) {
+                                            float* sd, float* R, float* X, float* F0, Emit& emit) {
   const int lane = gtid & 31, gw = gtid >> 5;
   const int kk = odd_ceil_dev((n + gt - 1) / gt);
   const int r0 = gtid * kk;
@@ -142,27 +329,95 @@ __device__ __forceinline__ void group_solve(int n, int gt, int bar, int gtid, fl
     group_sync(bar, gt);
     sl = gtid > 0 ? X[gtid - 1] : 0.f;
   }
-  chunk_back_smem<float>(kr, sj, sl, sa + r0, sc + r0, sd + r0, xg + r0);
-  if (gt != 32) group_sync(bar, gt);  // F0 / R / X reused by the next item
+  auto em = [&](int i, float v) { emit(r0 + i, v); };
+  chunk_back_smem<float>(kr, sj, sl, sa + r0, sc + r0, sd + r0, em);
+  if (gt != 32) group_sync(bar, gt);  // F0 / R / X reused by the next solve
 }
 
-// A BIG system (rows read straight from global memory): kBigSepRows chunks,
-// kBigChunks per consumer thread; their separators solved by PCR across the
-// consumers in shared memory, then every chunk eliminated again and
-// substituted back.
-__device__ __forceinline__ void solve_big(RagSys sy, const float* __restrict__ a, const float* __restrict__ b,
-                                       const float* __restrict__ c, const float* __restrict__ d, float* x, int tid,
-                                       float* Rsh, float* Xsh, float* Fb) {
+struct EmitStore {
+  float* x;
+  __device__ __forceinline__ void operator()(int i, float v) { x[i] = v; }
+};
+
+// Plain solve of one staged system by its group: x_i lands in the ring's b
+// slot of row i (b is not read by the back substitution), then the group
+// copies the rows out in order, so every warp store is one contiguous run.
+__device__ __forceinline__ void group_solve_plain(int n, int gt, int bar, int gtid, float* sa, float* sb, float* sc,
+                                                  float* sd, float* R, float* X, float* F0, float* xg) {
+  EmitStore em{sb};
+  group_solve(n, gt, bar, gtid, sa, sb, sc, sd, R, X, F0, em);
+  gsync(bar, gt);
+  for (int i = gtid; i < n; i += gt) xg[i] = sb[i];
+}
+// x_i = v on the first solve, x_i += v on the corrections.
+template <int MODE>
+struct EmitX {
+  XStore<MODE> xs;
+  bool first;
+  __device__ __forceinline__ void operator()(int i, float v) {
+    if (first)
+      xs.init(i, v);
+    else
+      xs.add(i, v);
+  }
+};
+
+// Refinement of one staged system by its solve group (see the file comment).
+// sa..sd: the system's rows in the ring, xh / xl: its x words in the ring.
+template <int MODE>
+__device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& sy, int gt, int bar, int gtid,
+                                             float* sa, const float* sb, float* sc, float* sd, float* xh, float* xl,
+                                             float* R, float* X, float* F0, double* red) {
   const int n = sy.n;
-  constexpr int KC = 17;
-  constexpr int NS = kBigSepRows;  // chunks (= separators) of the system
+  const float* ga = p.a + sy.off;
+  const float* gb = p.b + sy.off;
+  const float* gc = p.c + sy.off;
+  const float* gd = p.d + sy.off;
+  XStore<MODE> xs{xh, xl};
+  for (int sw = -1; sw < p.sweeps; ++sw) {  // sw = -1: the first solve
+    if (sw >= 0) {
+      gsync(bar, gt);  // every x_i written, every eliminated row read
+      for (int i = gtid; i < n; i += gt) {
+        const float a = ga[i], b = gb[i], c = gc[i], d = gd[i];
+        sa[i] = a;
+        sc[i] = c;
+        sd[i] = xs.residual(i, n, a, b, c, d);
+      }
+      gsync(bar, gt);
+    }
+    EmitX<MODE> em{xs, sw < 0};
+    group_solve(n, gt, bar, gtid, sa, sb, sc, sd, R, X, F0, em);
+  }
+  gsync(bar, gt);
+  float rr = 0.f, dd = 0.f;
+  double* xo = p.x64 + sy.off;
+  for (int i = gtid; i < n; i += gt) {
+    const float d = gd[i];
+    const float r = xs.residual(i, n, ga[i], gb[i], gc[i], d);
+    rr = fmaf(r, r, rr);
+    dd = fmaf(d, d, dd);
+    xo[i] = xs.get64(i);
+  }
+  group_rel_max(rr, dd, gt, bar, gtid, red, p.rel);
+}
+
+// A BIG system (rows read straight from global memory, right-hand side rhs):
+// kBigSepRows chunks, kBigChunks per consumer thread; their separators solved
+// by PCR across the consumers in shared memory, then every chunk eliminated
+// again and substituted back, emit(i, x_i).  Scratch: separator rows Ra..Rd,
+// their solution Xs, the chunks' first-row coefficients FD, FC, FA (kBigSepRows
+// floats each).
+template <class Emit>
+__device__ __forceinline__ void solve_big(const RagSys& sy, const float* __restrict__ ga,
+                                          const float* __restrict__ gb, const float* __restrict__ gc,
+                                          const float* __restrict__ gd, int tid, float* Ra, float* Rb, float* Rc,
+                                          float* Rd, float* Xs, float* FD, float* FC, float* FA, Emit& emit) {
+  const int n = sy.n;
+  constexpr int KC = kBigKC;
+  constexpr int NS = kBigSepRows;
   const int kk = odd_ceil_dev((n + NS - 1) / NS);
-  const float* ga = a + sy.off;
-  const float* gb = b + sy.off;
-  const float* gc = c + sy.off;
-  const float* gd = d + sy.off;
-  // pass 1: eliminate every chunk; export its first-row coefficients (Fb)
-  // and the part of its separator row that needs no neighbour (Rsh)
+  // pass 1: eliminate every chunk; export its first-row coefficients and the
+  // part of its separator row that needs no neighbour
 #pragma unroll 1
   for (int q = 0; q < kBigChunks; ++q) {
     const int j = q * kRagThreads + tid;
@@ -170,50 +425,43 @@ __device__ __forceinline__ void solve_big(RagSys sy, const float* __restrict__ a
     int kr = n - r0;
     kr = kr < 0 ? 0 : (kr > kk ? kk : kr);
     Chunk<float, KC> ch;
-    chunk_eliminate<float, KC>(ch, kr, j == 0, r0 + kr == n && kr > 0, ga + r0, gb + r0, gc + r0,
-                                     gd + r0);
-    Fb[3 * j + 0] = ch.fD; Fb[3 * j + 1] = ch.fC; Fb[3 * j + 2] = ch.fA;
+    chunk_eliminate<float, KC>(ch, kr, j == 0, r0 + kr == n && kr > 0, ga + r0, gb + r0, gc + r0, gd + r0);
+    FD[j] = ch.fD; FC[j] = ch.fC; FA[j] = ch.fA;
     const Row<float>& e = ch.sep;
-    Rsh[j] = -e.a * ch.lA; Rsh[NS + j] = e.b - e.a * ch.lC; Rsh[2 * NS + j] = e.c;
-    Rsh[3 * NS + j] = e.d - e.a * ch.lD;
+    Ra[j] = -e.a * ch.lA; Rb[j] = e.b - e.a * ch.lC; Rc[j] = e.c; Rd[j] = e.d - e.a * ch.lD;
   }
   consumer_sync(kRagThreads);
   // separator rows (the next chunk's first row folded in); PCR over all NS
-  // of them, kBigChunks rows per thread
   Row<float> sr[kBigChunks];
 #pragma unroll
   for (int q = 0; q < kBigChunks; ++q) {
     const int j = q * kRagThreads + tid;
-    const float nD = j + 1 < NS ? Fb[3 * (j + 1) + 0] : 0.f;
-    const float nC = j + 1 < NS ? Fb[3 * (j + 1) + 1] : 0.f;
-    const float nA = j + 1 < NS ? Fb[3 * (j + 1) + 2] : 0.f;
-    const float ec = Rsh[2 * NS + j];
-    sr[q] = Row<float>{Rsh[j], Rsh[NS + j] - ec * nA, -ec * nC, Rsh[3 * NS + j] - ec * nD};
+    const float nD = j + 1 < NS ? FD[j + 1] : 0.f;
+    const float nC = j + 1 < NS ? FC[j + 1] : 0.f;
+    const float nA = j + 1 < NS ? FA[j + 1] : 0.f;
+    const float ec = Rc[j];
+    sr[q] = Row<float>{Ra[j], Rb[j] - ec * nA, -ec * nC, Rd[j] - ec * nD};
   }
-  consumer_sync(kRagThreads);  // every partial row read before PCR overwrites Rsh
+  consumer_sync(kRagThreads);  // every partial row read before PCR overwrites them
   const Row<float> id{0.f, 1.f, 0.f, 0.f};
   for (int dl = 1; dl < NS; dl *= 2) {
 #pragma unroll
     for (int q = 0; q < kBigChunks; ++q) {
       const int j = q * kRagThreads + tid;
-      Rsh[j] = sr[q].a; Rsh[NS + j] = sr[q].b; Rsh[2 * NS + j] = sr[q].c; Rsh[3 * NS + j] = sr[q].d;
+      Ra[j] = sr[q].a; Rb[j] = sr[q].b; Rc[j] = sr[q].c; Rd[j] = sr[q].d;
     }
     consumer_sync(kRagThreads);
 #pragma unroll
     for (int q = 0; q < kBigChunks; ++q) {
       const int j = q * kRagThreads + tid;
-      const Row<float> L = j >= dl ? Row<float>{Rsh[j - dl], Rsh[NS + j - dl], Rsh[2 * NS + j - dl],
-                                                Rsh[3 * NS + j - dl]}
-                                   : id;
-      const Row<float> R = j + dl < NS ? Row<float>{Rsh[j + dl], Rsh[NS + j + dl], Rsh[2 * NS + j + dl],
-                                                    Rsh[3 * NS + j + dl]}
-                                       : id;
+      const Row<float> L = j >= dl ? Row<float>{Ra[j - dl], Rb[j - dl], Rc[j - dl], Rd[j - dl]} : id;
+      const Row<float> R = j + dl < NS ? Row<float>{Ra[j + dl], Rb[j + dl], Rc[j + dl], Rd[j + dl]} : id;
       sr[q] = reduce_row(sr[q], L, R);
     }
     consumer_sync(kRagThreads);
   }
 #pragma unroll
-  for (int q = 0; q < kBigChunks; ++q) Xsh[q * kRagThreads + tid] = tdiv(sr[q].d, sr[q].b);
+  for (int q = 0; q < kBigChunks; ++q) Xs[q * kRagThreads + tid] = tdiv(sr[q].d, sr[q].b);
   consumer_sync(kRagThreads);
   // pass 2: eliminate again and substitute back
 #pragma unroll 1
@@ -223,33 +471,64 @@ __device__ __forceinline__ void solve_big(RagSys sy, const float* __restrict__ a
     int kr = n - r0;
     kr = kr < 0 ? 0 : (kr > kk ? kk : kr);
     Chunk<float, KC> ch;
-    chunk_eliminate<float, KC>(ch, kr, j == 0, r0 + kr == n && kr > 0, ga + r0, gb + r0, gc + r0,
-                                     gd + r0);
-    chunk_back_store<float, KC>(ch, kr, Xsh[j], j > 0 ? Xsh[j - 1] : 0.f, x + sy.off + r0);
+    chunk_eliminate<float, KC>(ch, kr, j == 0, r0 + kr == n && kr > 0, ga + r0, gb + r0, gc + r0, gd + r0);
+    auto em = [&](int i, float v) { emit(r0 + i, v); };
+    chunk_back_emit<float, KC>(ch, kr, Xs[j], j > 0 ? Xs[j - 1] : 0.f, em);
   }
-  consumer_sync(kRagThreads);  // Fb / Xsh reused by the next item
+  consumer_sync(kRagThreads);  // scratch reused by the next solve
 }
 
+// Refinement of a BIG system by the whole CTA; x and r in the global scratch.
+template <int MODE>
+__device__ __forceinline__ void big_refine(const RagParams& p, const RagSys& sy, int tid, float* Ra, float* Rb,
+                                           float* Rc, float* Rd, float* Xs, float* FD, float* FC, float* FA,
+                                           double* red) {
+  const int n = sy.n;
+  const float* ga = p.a + sy.off;
+  const float* gb = p.b + sy.off;
+  const float* gc = p.c + sy.off;
+  const float* gd = p.d + sy.off;
+  float* wr = p.wr + sy.off;
+  XStore<MODE> xs{p.wxh + sy.off, p.wxl + sy.off};
+  for (int sw = -1; sw < p.sweeps; ++sw) {  // sw = -1: the first solve
+    if (sw >= 0) {
+      for (int i = tid; i < n; i += kRagThreads) wr[i] = xs.residual(i, n, ga[i], gb[i], gc[i], gd[i]);
+      consumer_sync(kRagThreads);
+    }
+    EmitX<MODE> em{xs, sw < 0};
+    solve_big(sy, ga, gb, gc, sw < 0 ? gd : wr, tid, Ra, Rb, Rc, Rd, Xs, FD, FC, FA, em);
+  }
+  float rr = 0.f, dd = 0.f;
+  double* xo = p.x64 + sy.off;
+  for (int i = tid; i < n; i += kRagThreads) {
+    const float d = gd[i];
+    const float r = xs.residual(i, n, ga[i], gb[i], gc[i], d);
+    rr = fmaf(r, r, rr);
+    dd = fmaf(d, d, dd);
+    xo[i] = xs.get64(i);
+  }
+  group_rel_max(rr, dd, kRagThreads, 1, tid, red, p.rel);
+  consumer_sync(kRagThreads);
+}
+
+// ---------------------------------------------------------------------------
+template <int MODE>
 __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p) {
   static_assert((kRagThreads + 32) % 128 == 0, "16 warps: 4 per SM sub-partition");
+  constexpr int RR = ring_rows(MODE);
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
-  uint64_t* empty = full + 2;
-  RagStage* desc = reinterpret_cast<RagStage*>(smem + 64);
-  float* buf = reinterpret_cast<float*>(smem + 64 + 2 * sizeof(RagStage) + 64 - ((64 + 2 * sizeof(RagStage)) % 64));
-  // buf layout: array q (a, b, c, d) occupies [q * 2 * kStageRows, (q+1) * 2 * kStageRows);
-  // stage s is the half [s * kStageRows, (s+1) * kStageRows) of every array.
-  float* Rsh = buf + 4 * 2 * kStageRows;  // group / CTA separators: 4 x kRagThreads
-  float* Xsh = Rsh + 4 * kRagThreads;     // their solution
-  float* F0 = Xsh + kRagThreads;          // lane-0 first-row coefficients of each warp (3 x kRagWarps)
-  // A BIG item stages nothing: its separators (4 x kBigSepRows) use the a-half
-  // of its stage, their solution and the chunks' first-row coefficients
-  // (kBigSepRows + 3 x kBigSepRows) the b-half.
-  static_assert(4 * kBigSepRows <= kStageRows, "BIG scratch fits the halves of one stage");
+  uint64_t* empty = full + kSlots;
+  RagSlot* desc = reinterpret_cast<RagSlot*>(smem + 2 * kSlots * 8);
+  float* Rsh = reinterpret_cast<float*>(smem + kHeadBytes);  // group / CTA separators: 4 x kRagThreads
+  float* Xsh = Rsh + 4 * kRagThreads;                           // their solution
+  float* F0 = Xsh + kRagThreads;                                // lane-0 first-row coefficients (3 per warp)
+  double* red = reinterpret_cast<double*>(F0 + 48);             // norms: 2 per warp
+  float* ring = Rsh + kGroupFloats;                             // array q at ring + q * RR
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if (tid == 0) {
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < kSlots; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], kRagWarps);
     }
@@ -257,112 +536,172 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
   }
   __syncthreads();
 
-  if (tid >= kRagThreads) {  // ---------------- producer ----------------
-    if (lane != 0) return;
-    int k = 0;  // slot counter; slot k uses stage k & 1
-    bool done = false;
-    int next = blockIdx.x;
-    while (!done) {
-      int item = next < p.nitems ? next : -1;
-      next += gridDim.x;
-      const int kind = item >= 0 ? p.items[item].kind : (int)kEnd;
-      if (kind == kDouble && (k & 1)) {  // a DOUBLE starts on stage 0: pad with a NOP
-        if (k >= 2 && !mbar_wait(&empty[1], ((k >> 1) - 1) & 1, p.status)) break;
-        desc[1].item = -1;
-        desc[1].kind = kNop;
-        mbar_arrive(&full[1]);
-        ++k;
+  if (tid >= kRagThreads) {  // ---------------- producer warp ----------------
+    // Every lane runs the same control flow; lane q handles system q of an
+    // item (its descriptor entry and its four bulk copies), lane 0 the
+    // item-wide fields and the arrive.
+    int k = 0;       // items published
+    int oldest = 0;  // oldest item not yet reclaimed
+    int head = 0;    // next free ring row
+    RagItem nxt{kEnd, 0, 0, 0};
+    if ((int)blockIdx.x < p.nitems) nxt = p.items[blockIdx.x];
+    for (int item = blockIdx.x;; item += gridDim.x) {
+      const bool end = item >= p.nitems;
+      const RagItem it = nxt;
+      if (item + (int)gridDim.x < p.nitems) nxt = p.items[item + gridDim.x];  // next item's record, early
+      int kind = end ? (int)kEnd : it.kind;
+      if (kind == kSingle && it.rows > RR) kind = kBig;  // does not fit this mode's ring
+      RagSys sy{0, 0, 0};
+      if (!end && lane < it.count) sy = p.sys[it.first + lane];
+      // ring rows of this lane's system and their exclusive prefix over lanes
+      const long lo = sy.off & ~3L, hi = (sy.off + sy.n + 3) & ~3L;
+      const int mine = (!end && kind != kBig && lane < it.count) ? (int)(hi - lo) : 0;
+      int pre = mine;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(kFull, pre, o);
+        if (lane >= o) pre += v;
       }
-      const int s = k & 1;
-      if (k >= 2 && !mbar_wait(&empty[s], ((k >> 1) - 1) & 1, p.status)) break;
-      // A DOUBLE (always on stage 0 here) also needs stage 1, last used at slot k-1.
-      if (kind == kDouble && k >= 1 && !mbar_wait(&empty[1], ((k - 1) >> 1) & 1, p.status)) break;
-      desc[s].item = item;
-      desc[s].kind = kind;
-      if (kind == kEnd) {
-        mbar_arrive(&full[s]);
-        done = true;
-        break;
+      const int need = end ? 0 : (kind == kBig ? kBigScratchRows : __shfl_sync(kFull, pre, 31));
+      pre -= mine;
+      // a free slot and `need` contiguous ring rows, reclaiming oldest first
+      int place = -1;
+      bool ok = true;
+      while (true) {
+        const int inflight = k - oldest;
+        if (inflight == 0) {
+          head = 0;
+          place = 0;
+          break;
+        }
+        if (inflight < kSlots) {
+          const int tail = desc[oldest % kSlots].rbase;
+          if (tail < head) {  // occupied [tail, head)
+            if (head + need <= RR) { place = head; break; }
+            if (need <= tail) { place = 0; break; }
+          } else if (head + need <= tail) {  // occupied [tail, RR) and [0, head)
+            place = head;
+            break;
+          }
+        }
+        // lane 0 waits (bounded); the verdict is the warp's, and every lane
+        // then acquires the completed phase itself
+        bool w = true;
+        if (lane == 0) w = mbar_wait(&empty[oldest % kSlots], (oldest / kSlots) & 1, p.status);
+        if (!__shfl_sync(kFull, (int)w, 0)) {
+          ok = false;
+          break;
+        }
+        mbar_try_wait(&empty[oldest % kSlots], (oldest / kSlots) & 1);
+        ++oldest;
       }
-      if (kind == kBig) {  // rows are read from global memory by the consumers
-        mbar_arrive(&full[s]);
-        ++k;
-        continue;
+      if (!ok) break;  // consumers time out on their own waits
+      const int s = k % kSlots;
+      __syncwarp();  // every lane has read desc[oldest].rbase before slot s is rewritten
+      if (lane < (end ? 0 : it.count)) {
+        desc[s].off[lane] = sy.off;
+        desc[s].n[lane] = sy.n;
+        desc[s].base[lane] = kind == kBig ? place : place + pre + (int)(sy.off - lo);
       }
-      const RagItem it = p.items[item];
-      // Bytes of the whole item first: the single arrive carries the full
-      // transaction count, so the phase cannot complete before every copy.
-      uint32_t tx = 0;
-      int cursor = s * kStageRows;
-      for (int q = 0; q < it.count; ++q) {
-        const RagSys sy = p.sys[it.first + q];
-        const long lo = sy.off & ~3L, hi = (sy.off + sy.n + 3) & ~3L;
-        desc[s].base[q] = cursor + (int)(sy.off - lo);
-        tx += 4u * (uint32_t)((hi - lo) * 4);
-        cursor += (int)(hi - lo);
+      if (lane == 0) {
+        desc[s].kind = kind;
+        desc[s].count = end ? 0 : it.count;
+        desc[s].rbase = place;
+        desc[s].rrows = need;
       }
-      mbar_arrive_expect_tx(&full[s], tx);
-      cursor = s * kStageRows;
-      for (int q = 0; q < it.count; ++q) {
-        const RagSys sy = p.sys[it.first + q];
-        const long lo = sy.off & ~3L, hi = (sy.off + sy.n + 3) & ~3L;
-        const uint32_t bytes = (uint32_t)((hi - lo) * 4);
-        bulk_g2s(buf + 0 * 2 * kStageRows + cursor, p.a + lo, bytes, &full[s]);
-        bulk_g2s(buf + 1 * 2 * kStageRows + cursor, p.b + lo, bytes, &full[s]);
-        bulk_g2s(buf + 2 * 2 * kStageRows + cursor, p.c + lo, bytes, &full[s]);
-        bulk_g2s(buf + 3 * 2 * kStageRows + cursor, p.d + lo, bytes, &full[s]);
-        cursor += (int)(hi - lo);
+      __syncwarp();  // the descriptor is complete before lane 0 publishes it
+      if (lane == 0) {
+        // bytes of the whole item in the one arrive: the phase cannot
+        // complete before every copy has landed
+        if (end || kind == kBig)
+          mbar_arrive(&full[s]);
+        else
+          mbar_arrive_expect_tx(&full[s], 16u * (uint32_t)need);
       }
+      if (end) break;
+      __syncwarp();
+      if (mine > 0) {
+        const uint32_t bytes = 4u * (uint32_t)mine;
+        const int cur = place + pre;
+        bulk_g2s(ring + 0 * RR + cur, p.a + lo, bytes, &full[s]);
+        bulk_g2s(ring + 1 * RR + cur, p.b + lo, bytes, &full[s]);
+        bulk_g2s(ring + 2 * RR + cur, p.c + lo, bytes, &full[s]);
+        bulk_g2s(ring + 3 * RR + cur, p.d + lo, bytes, &full[s]);
+      }
+      head = place + need;
       ++k;
-      if (kind == kDouble) {  // the second buffer belongs to this item: publish a continuation
-        desc[1].item = -1;
-        desc[1].kind = kCont;
-        mbar_arrive(&full[1]);
-        ++k;
-      }
     }
     return;
   }
 
   // ---------------- consumers ----------------
-  float* A = buf;  // the consumers overwrite a, c, d of a staged item in place
-  const float* B = buf + 2 * kStageRows;
-  float* C = buf + 4 * kStageRows;
-  float* D = buf + 6 * kStageRows;
+  float* A = ring;  // the consumers overwrite a, c, d (and, plain, b with x) of a staged item in place
+  float* B = ring + RR;
+  float* C = ring + 2 * RR;
+  float* D = ring + 3 * RR;
+  float* XH = ring + 4 * RR;  // refined modes: x words
+  float* XL = ring + 5 * RR;
   for (int k = 0;; ++k) {
-    const int s = k & 1;
-    const bool ok = consumer_sync_and(kRagThreads, mbar_wait(&full[s], (k >> 1) & 1, p.status));
+    const int s = k % kSlots;
+    const bool ok = consumer_sync_and(kRagThreads, mbar_wait(&full[s], (k / kSlots) & 1, p.status));
     if (!ok) break;
-    const int kind = desc[s].kind;
+    const RagSlot& ds = desc[s];
+    const int kind = ds.kind;
     if (kind == kEnd) break;
     if (kind == kMulti) {
-      const RagItem it = p.items[desc[s].item];
-      if (warp < it.count) {
-        const RagSys sy = p.sys[it.first + warp];
-        const int base = desc[s].base[warp];
-        group_solve(sy.n, 32, 0, lane, A + base, B + base, C + base, D + base, nullptr, nullptr, nullptr,
-                    p.x + sy.off);
+      if (warp < ds.count) {
+        const RagSys sy{ds.off[warp], ds.n[warp], 0};
+        const int base = ds.base[warp];
+        if constexpr (MODE == kPlain) {
+          group_solve_plain(sy.n, 32, 0, lane, A + base, B + base, C + base, D + base, nullptr, nullptr, nullptr,
+                            p.x + sy.off);
+        } else {
+          group_refine<MODE>(p, sy, 32, 0, lane, A + base, B + base, C + base, D + base, XH + base, XL + base,
+                             nullptr, nullptr, nullptr, red);
+        }
       }
     } else if (kind == kMulti4) {
-      const RagItem it = p.items[desc[s].item];
       const int g = tid / kGroup4Threads;
-      if (g < it.count) {
-        const RagSys sy = p.sys[it.first + g];
-        const int base = desc[s].base[g];
-        group_solve(sy.n, kGroup4Threads, 2 + g, tid - g * kGroup4Threads, A + base, B + base, C + base, D + base,
-                    Rsh + g * 4 * kGroup4Threads, Xsh + g * kGroup4Threads, F0 + g * 3 * (kGroup4Threads / 32),
-                    p.x + sy.off);
+      if (g < ds.count) {
+        const RagSys sy{ds.off[g], ds.n[g], 0};
+        const int base = ds.base[g];
+        const int gtid = tid - g * kGroup4Threads;
+        float* R = Rsh + g * 4 * kGroup4Threads;
+        float* X = Xsh + g * kGroup4Threads;
+        float* F = F0 + g * 3 * (kGroup4Threads / 32);
+        if constexpr (MODE == kPlain) {
+          group_solve_plain(sy.n, kGroup4Threads, 2 + g, gtid, A + base, B + base, C + base, D + base, R, X, F,
+                            p.x + sy.off);
+        } else {
+          group_refine<MODE>(p, sy, kGroup4Threads, 2 + g, gtid, A + base, B + base, C + base, D + base, XH + base,
+                             XL + base, R, X, F, red);
+        }
       }
-    } else if (kind == kSingle || kind == kDouble) {
-      const RagItem it = p.items[desc[s].item];
-      const RagSys sy = p.sys[it.first];
-      const int base = desc[s].base[0];
-      group_solve(sy.n, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, Rsh, Xsh, F0, p.x + sy.off);
-    } else if (kind == kBig) {
-      const RagItem it = p.items[desc[s].item];
-      float* bR = buf + s * kStageRows;
-      float* bX = buf + 2 * kStageRows + s * kStageRows;
-      solve_big(p.sys[it.first], p.a, p.b, p.c, p.d, p.x, tid, bR, bX, bX + kBigSepRows);
+    } else if (kind == kSingle) {
+      const RagSys sy{ds.off[0], ds.n[0], 0};
+      const int base = ds.base[0];
+      if constexpr (MODE == kPlain) {
+        group_solve_plain(sy.n, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, Rsh, Xsh, F0,
+                          p.x + sy.off);
+      } else {
+        group_refine<MODE>(p, sy, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, XH + base, XL + base,
+                           Rsh, Xsh, F0, red);
+      }
+    } else {  // kBig
+      const RagSys sy{ds.off[0], ds.n[0], 0};
+      const int rb = ds.rbase;
+      float* Ra = A + rb;
+      float* Rb = ring + RR + rb;
+      float* Rc = C + rb;
+      float* Rd = D + rb;
+      if constexpr (MODE == kPlain) {
+        EmitStore em{p.x + sy.off};
+        solve_big(sy, p.a + sy.off, p.b + sy.off, p.c + sy.off, p.d + sy.off, tid, Ra, Rb, Rc, Rd,
+                  Ra + kBigSepRows, Rb + kBigSepRows, Rc + kBigSepRows, Rd + kBigSepRows, em);
+      } else {
+        big_refine<MODE>(p, sy, tid, Ra, Rb, Rc, Rd, Ra + kBigSepRows, Rb + kBigSepRows, Rc + kBigSepRows,
+                         Rd + kBigSepRows, red);
+      }
     }
     release_stage(&empty[s]);
   }
@@ -381,11 +720,6 @@ struct RaggedPlan {
 };
 
 namespace {
-size_t rag_smem_bytes() {
-  size_t head = 64 + 2 * sizeof(RagStage);
-  head += 64 - head % 64;
-  return head + (size_t)(4 * 2 * kStageRows + 5 * kRagThreads + 3 * kRagWarps) * sizeof(float);
-}
 long padded_rows(long off, int n) { return ((off + n + 3) & ~3L) - (off & ~3L); }
 }  // namespace
 
@@ -416,39 +750,35 @@ tridi_status tridi_ragged_plan_create(const long* offsets, int num_systems, void
   });
   plan->sys.reserve(num_systems);
   for (int s : order) plan->sys.push_back(RagSys{offsets[s], (int)(offsets[s + 1] - offsets[s]), 0});
+  // threads per system: the autotuned choice for the system's size bucket,
+  // else 32 up to 480 rows, 160 up to 2400, the whole CTA above
+  auto threads_for = [](long n) {
+    const int t = tuned(TRIDI_AUTOTUNE_RAGGED_THREADS, ilog2(n));
+    if (t == 32 || t == kGroup4Threads || t == kRagThreads) return t;
+    return n <= kWarpMaxRows ? 32 : (n <= kGroup4MaxRows ? kGroup4Threads : kRagThreads);
+  };
+  constexpr long kPackCap = ring_rows(kRefineDF);  // a packed item fits the ring of every mode
   int i = 0;
   while (i < num_systems) {
     const RagSys& sy = plan->sys[i];
     const long pr = padded_rows(sy.off, sy.n);
-    if (sy.n > kMaxSystemRows || pr > 2 * kStageRows) {
+    if (pr > kMaxStagedRows) {
       plan->items.push_back(RagItem{(int)kBig, 1, i, 0});
       ++i;
       continue;
     }
-    if (sy.n > kGroup4MaxRows) {
-      RagItem it{pr > kStageRows ? (int)kDouble : (int)kSingle, 1, i, (int)pr};
-      plan->items.push_back(it);
+    const int th = pr > kPackCap ? kRagThreads : threads_for(sy.n);
+    if (th == kRagThreads) {
+      plan->items.push_back(RagItem{(int)kSingle, 1, i, (int)pr});
       ++i;
       continue;
     }
-    if (sy.n > kWarpMaxRows) {
-      RagItem it{(int)kMulti4, 0, i, 0};
-      while (i < num_systems && it.count < kRagThreads / kGroup4Threads) {
-        const RagSys& t = plan->sys[i];
-        const long tr = padded_rows(t.off, t.n);
-        if (t.n > kGroup4MaxRows || t.n <= kWarpMaxRows || it.rows + tr > kStageRows) break;
-        it.rows += (int)tr;
-        ++it.count;
-        ++i;
-      }
-      plan->items.push_back(it);
-      continue;
-    }
-    RagItem it{(int)kMulti, 0, i, 0};
-    while (i < num_systems && it.count < kMaxItemSystems) {
+    RagItem it{th == 32 ? (int)kMulti : (int)kMulti4, 0, i, 0};
+    const int cap = th == 32 ? kMaxItemSystems : kRagThreads / kGroup4Threads;
+    while (i < num_systems && it.count < cap) {
       const RagSys& t = plan->sys[i];
       const long tr = padded_rows(t.off, t.n);
-      if (t.n > kWarpMaxRows || it.rows + tr > kStageRows) break;
+      if (tr > kPackCap || threads_for(t.n) != th || it.rows + tr > kPackCap) break;
       it.rows += (int)tr;
       ++it.count;
       ++i;
@@ -520,38 +850,96 @@ tridi_status tridi_ragged_plan_destroy(void* plan) {
   return TRIDI_SUCCESS;
 }
 
+}  // extern "C"
+
+namespace tridi {
+namespace {
+
+template <int MODE>
+tridi_status ragged_launch(const RaggedPlan* plan, void* dev_plan, RagParams& p, cudaStream_t st) {
+  const DeviceInfo* dev = current_device();
+  if (!dev) return TRIDI_ERROR_CUDA;
+  const size_t smem = rag_smem_bytes(MODE);
+  if (smem > (size_t)dev->max_smem_optin) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(ragged_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+      cudaSuccess)
+    return cuda_status(e);
+  char* dp = static_cast<char*>(dev_plan);
+  p.items = reinterpret_cast<const RagItem*>(dp + 64);
+  p.sys = reinterpret_cast<const RagSys*>(dp + 64 + plan->items.size() * sizeof(RagItem));
+  p.nitems = (int)plan->items.size();
+  p.status = dev->status;
+  int grid = dev->sm_count;
+  if (grid > p.nitems) grid = p.nitems;
+  ragged_kernel<MODE><<<grid, kRagThreads + 32, smem, st>>>(p);
+  return cuda_status(cudaGetLastError());
+}
+
+long pad4(long v) { return (v + 3) & ~3L; }
+long a64(long v) { return (v + 63) & ~63L; }
+
+}  // namespace
+}  // namespace tridi
+
+extern "C" {
+
 // Solves every system of the plan.  a..d, x: concatenated rows (device,
 // 16-byte aligned, at least round_up(total_rows, 4) elements).  dev_plan: the
-// uploaded plan.  Stream-ordered; resets the work counter itself (a memset),
-// so the call can be captured in a CUDA graph and replayed.
+// uploaded plan.  Stream-ordered and free of host synchronisation, so the
+// call can be captured in a CUDA graph and replayed.
 tridi_status tridi_ragged_solve_f32(const float* a, const float* b, const float* c, const float* d, float* x,
                                     const void* plan_, void* dev_plan, tridi_stream_t stream) {
   using namespace tridi;
   const auto* plan = static_cast<const RaggedPlan*>(plan_);
   if (!a || !b || !c || !d || !x || !plan || !dev_plan) return TRIDI_ERROR_INVALID_VALUE;
   if (!aligned16(a) || !aligned16(b) || !aligned16(c) || !aligned16(d)) return TRIDI_ERROR_MISALIGNED;
-  const DeviceInfo* dev = current_device();
-  if (!dev) return TRIDI_ERROR_CUDA;
-  const size_t smem = rag_smem_bytes();
-  if (smem > (size_t)dev->max_smem_optin) return TRIDI_ERROR_UNSUPPORTED_SIZE;
-  cudaStream_t st = as_stream(stream);
-  cudaError_t e;
-  if ((e = cudaFuncSetAttribute(ragged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-      cudaSuccess)
-    return cuda_status(e);
-  char* dp = static_cast<char*>(dev_plan);
-  if ((e = cudaMemsetAsync(dp, 0, 64, st)) != cudaSuccess) return cuda_status(e);
   RagParams p{};
   p.a = a; p.b = b; p.c = c; p.d = d; p.x = x;
-  p.items = reinterpret_cast<const RagItem*>(dp + 64);
-  p.sys = reinterpret_cast<const RagSys*>(dp + 64 + plan->items.size() * sizeof(RagItem));
-  p.nitems = (int)plan->items.size();
-  p.counter = reinterpret_cast<unsigned*>(dp);
-  p.status = dev->status;
-  int grid = dev->sm_count;
-  if (grid > p.nitems) grid = p.nitems;
-  ragged_kernel<<<grid, kRagThreads + 32, smem, st>>>(p);
-  return cuda_status(cudaGetLastError());
+  return ragged_launch<kPlain>(plan, dev_plan, p, as_stream(stream));
+}
+
+// Workspace of tridi_ragged_refine_f32: x (two words) and r of systems too
+// large for the shared-memory ring, per row of the batch.
+size_t tridi_ragged_refine_workspace_bytes(long total_rows, long num_systems) {
+  (void)num_systems;
+  return (size_t)tridi::a64(tridi::pad4(total_rows)) * 12 + 256;
+}
+
+// Fused refinement of every system of the plan (see the file comment):
+// FP32 solves in shared memory, residual and accumulation in extended
+// precision (TRIDI_TUNE_RESIDUAL: double-float by default, native FP64 on
+// request), `sweeps` corrections, x written once in FP64.  *dev_rel (device
+// double) receives max over systems of ||d - T x||_2 / ||d||_2.  offsets_dev
+// is accepted for interface stability and not needed.  Stream-ordered, no
+// host synchronisation (capturable in a CUDA graph).
+tridi_status tridi_ragged_refine_f32(const float* a, const float* b, const float* c, const float* d, double* x,
+                                     const void* plan_, void* dev_plan, const long* offsets_dev, int sweeps,
+                                     void* ws, size_t ws_bytes, double* dev_rel, tridi_stream_t stream) {
+  using namespace tridi;
+  (void)offsets_dev;
+  const auto* plan = static_cast<const RaggedPlan*>(plan_);
+  if (!a || !b || !c || !d || !x || !plan || !dev_plan || !ws || !dev_rel || sweeps < 0)
+    return TRIDI_ERROR_INVALID_VALUE;
+  if (!aligned16(a) || !aligned16(b) || !aligned16(c) || !aligned16(d)) return TRIDI_ERROR_MISALIGNED;
+  const long total = plan->total_rows;
+  if (ws_bytes < tridi_ragged_refine_workspace_bytes(total, plan->num_systems))
+    return TRIDI_ERROR_WORKSPACE_TOO_SMALL;
+  const long rows = a64(pad4(total));
+  cudaStream_t st = as_stream(stream);
+  cudaError_t ce;
+  if ((ce = cudaMemsetAsync(dev_rel, 0, sizeof(double), st)) != cudaSuccess) return cuda_status(ce);
+  RagParams p{};
+  p.a = a; p.b = b; p.c = c; p.d = d; p.x64 = x;
+  p.wxh = static_cast<float*>(ws);
+  p.wxl = p.wxh + rows;
+  p.wr = p.wxl + rows;
+  p.rel = reinterpret_cast<unsigned long long*>(dev_rel);
+  p.sweeps = sweeps;
+  const int res = tunable(TRIDI_TUNE_RESIDUAL);
+  if (res == TRIDI_RESIDUAL_FP64) return ragged_launch<kRefineFP64>(plan, dev_plan, p, st);
+  if (res != 0 && res != TRIDI_RESIDUAL_DF) return TRIDI_ERROR_INVALID_VALUE;
+  return ragged_launch<kRefineDF>(plan, dev_plan, p, st);
 }
 
 }  // extern "C"

@@ -200,7 +200,8 @@ RefineWs carve(void* ws, long n, long m, int layout) {
 
 int default_rest(int n) {
   const int t = tunable(TRIDI_TUNE_CRPCR_REST);
-  int rest = t > 0 ? t : 4;
+  const int a = tuned(TRIDI_AUTOTUNE_CRPCR_REST, ilog2(n));
+  int rest = t > 0 ? t : (a > 0 ? a : 4);
   while (rest > n / 2 && rest > 2) rest /= 2;
   return rest;
 }
@@ -286,136 +287,6 @@ tridi_status tridi_refine_f32(const float* a, const float* b, const float* c, co
                               long m, int layout, double tol, int max_sweeps, void* ws, size_t ws_bytes,
                               tridi_stream_t s, int* sweeps, double* rel_residual) {
   return tridi::refine_device(a, b, c, d, x, n, m, layout, tol, max_sweeps, ws, ws_bytes, s, sweeps, rel_residual);
-}
-
-}  // extern "C"
-
-// ---------------------------------------------------------------------------
-// Ragged batches: the same update + residual with one block per system
-// (rows [off[s], off[s] + n[s]) of the concatenated arrays), so each system's
-// norms are plain block reductions.  Used by tridi_ragged_refine_f32.
-namespace tridi {
-
-struct RaggedRefineParams {
-  const float *a, *b, *c, *d;
-  const float* e;
-  const double* xin;
-  double* xout;
-  float* r;
-  double* rr;
-  double* dd;
-  const long* off;  // num_systems + 1 row offsets (device)
-  int first;
-};
-
-__global__ void __launch_bounds__(256) refine_ragged_kernel(RaggedRefineParams p) {
-  const long s = blockIdx.x;
-  const long lo = p.off[s], n = p.off[s + 1] - lo;
-  double rs = 0.0, ds = 0.0;
-  for (long i = threadIdx.x; i < n; i += blockDim.x) {
-    const long k = lo + i;
-    const double xi = p.first ? (double)p.e[k] : p.xin[k] + (double)p.e[k];
-    const double di = (double)p.d[k];
-    double r = di - (double)p.b[k] * xi;
-    if (i > 0) r -= (double)p.a[k] * (p.first ? (double)p.e[k - 1] : p.xin[k - 1] + (double)p.e[k - 1]);
-    if (i < n - 1) r -= (double)p.c[k] * (p.first ? (double)p.e[k + 1] : p.xin[k + 1] + (double)p.e[k + 1]);
-    p.xout[k] = xi;
-    p.r[k] = (float)r;
-    rs += r * r;
-    ds += di * di;
-  }
-  __shared__ double red[2][8];
-  for (int o = 16; o > 0; o >>= 1) {
-    rs += __shfl_down_sync(kFull, rs, o);
-    ds += __shfl_down_sync(kFull, ds, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    red[0][threadIdx.x >> 5] = rs;
-    red[1][threadIdx.x >> 5] = ds;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a0 = 0, a1 = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      a0 += red[0][w];
-      a1 += red[1][w];
-    }
-    p.rr[s] = a0;
-    if (p.first) p.dd[s] = a1;
-  }
-}
-
-}  // namespace tridi
-
-extern "C" tridi_status tridi_ragged_solve_f32(const float* a, const float* b, const float* c, const float* d,
-                                               float* x, const void* plan, void* dev_plan, tridi_stream_t stream);
-extern "C" long tridi_ragged_plan_total_rows(const void* plan);
-extern "C" int tridi_ragged_plan_num_systems(const void* plan);
-
-namespace {
-long pad4(long v) { return (v + 3) & ~3L; }
-long a64(long v) { return (v + 63) & ~63L; }
-}  // namespace
-
-extern "C" {
-
-// Workspace of tridi_ragged_refine_f32 for a plan of `total_rows` rows and
-// `num_systems` systems.
-size_t tridi_ragged_refine_workspace_bytes(long total_rows, long num_systems) {
-  const long rows = a64(pad4(total_rows));
-  return (size_t)rows * (4 + 4 + 8) + (size_t)a64(num_systems + 1) * (8 + 8 + 8) + 256 + 1024;
-}
-
-// FP32 ragged solves + FP64 residual / update, a FIXED number of corrections
-// (no host synchronisation, so the whole sequence can be captured in a CUDA
-// graph and replayed): x = e0; repeat `sweeps` times { r = d - T x;
-// e = solve(r); x += e }; a last residual pass writes the maximum relative
-// residual to *dev_rel (device double).  x (FP64, padded rows) must hold
-// round_up(total_rows, 4) elements.  offsets_dev: the plan's offsets on the
-// device (num_systems + 1 int64).
-tridi_status tridi_ragged_refine_f32(const float* a, const float* b, const float* c, const float* d, double* x,
-                                     const void* plan, void* dev_plan, const long* offsets_dev, int sweeps,
-                                     void* ws, size_t ws_bytes, double* dev_rel, tridi_stream_t stream) {
-  using namespace tridi;
-  if (!a || !b || !c || !d || !x || !plan || !dev_plan || !offsets_dev || !ws || !dev_rel || sweeps < 0)
-    return TRIDI_ERROR_INVALID_VALUE;
-  const long total = tridi_ragged_plan_total_rows(plan);
-  const long m = tridi_ragged_plan_num_systems(plan);
-  if (ws_bytes < tridi_ragged_refine_workspace_bytes(total, m)) return TRIDI_ERROR_WORKSPACE_TOO_SMALL;
-  const long rows = a64(pad4(total));
-  char* w = static_cast<char*>(ws);
-  float* e = reinterpret_cast<float*>(w); w += rows * 4;
-  float* r = reinterpret_cast<float*>(w); w += rows * 4;
-  double* xalt = reinterpret_cast<double*>(w); w += rows * 8;
-  double* rr = reinterpret_cast<double*>(w); w += a64(m + 1) * 8;
-  double* dd = reinterpret_cast<double*>(w); w += a64(m + 1) * 8;
-  cudaStream_t st = as_stream(stream);
-  cudaError_t ce;
-  // the pad rows of r are read by the bulk copies of the next solve: keep them defined
-  if ((ce = cudaMemsetAsync(r, 0, rows * 4, st)) != cudaSuccess) return cuda_status(ce);
-  tridi_status ts = tridi_ragged_solve_f32(a, b, c, d, e, plan, dev_plan, stream);
-  if (ts != TRIDI_SUCCESS) return ts;
-  RaggedRefineParams p{};
-  p.a = a; p.b = b; p.c = c; p.d = d; p.e = e; p.r = r; p.rr = rr; p.dd = dd; p.off = offsets_dev;
-  double* bufs[2] = {x, xalt};
-  int cur = 0;
-  for (int k = 0; k <= sweeps; ++k) {
-    p.first = k == 0;
-    p.xin = bufs[cur];
-    p.xout = k == 0 ? x : bufs[cur ^ 1];
-    refine_ragged_kernel<<<(unsigned)m, 256, 0, st>>>(p);
-    if ((ce = cudaGetLastError()) != cudaSuccess) return cuda_status(ce);
-    cur = p.xout == x ? 0 : 1;
-    if (k == sweeps) break;
-    ts = tridi_ragged_solve_f32(a, b, c, r, e, plan, dev_plan, stream);
-    if (ts != TRIDI_SUCCESS) return ts;
-  }
-  refine_maxrel_kernel<<<1, 1024, 0, st>>>(rr, dd, m, dev_rel);
-  if ((ce = cudaGetLastError()) != cudaSuccess) return cuda_status(ce);
-  if (cur != 0 && (ce = cudaMemcpyAsync(x, bufs[cur], sizeof(double) * total, cudaMemcpyDeviceToDevice, st)) !=
-                      cudaSuccess)
-    return cuda_status(ce);
-  return TRIDI_SUCCESS;
 }
 
 }  // extern "C"

@@ -15,6 +15,16 @@ int g_tunable[kTunables] = {};
 
 int tunable(int key) { return key >= 0 && key < kTunables ? g_tunable[key] : 0; }
 
+namespace {
+constexpr int kTuneTables = 3, kTuneKeys = 32;
+int g_tuned[kTuneTables][kTuneKeys] = {};
+}  // namespace
+
+int tuned(int table, int log2key) {
+  if (table < 0 || table >= kTuneTables || log2key < 0 || log2key >= kTuneKeys) return 0;
+  return g_tuned[table][log2key];
+}
+
 int pick_stages(size_t fixed_bytes, size_t stage_bytes, int fallback, const DeviceInfo& dev) {
   int S = tunable(TRIDI_TUNE_STAGES);
   if (S <= 0) S = fallback;
@@ -92,6 +102,25 @@ tridi_status tridi_set_tunable(int key, int value) {
 }
 
 int tridi_get_tunable(int key) { return tunable(key); }
+
+int tridi_tuned(int table, long key) {
+  if (key < 1) return 0;
+  return tridi::tuned(table, tridi::ilog2(key));
+}
+
+tridi_status tridi_set_tuned(int table, long key, int value) {
+  using namespace tridi;
+  if (table < 0 || table >= kTuneTables || key < 1 || ilog2(key) >= kTuneKeys || value < 0)
+    return TRIDI_ERROR_INVALID_VALUE;
+  g_tuned[table][ilog2(key)] = value;
+  return TRIDI_SUCCESS;
+}
+
+tridi_status tridi_autotune_reset(void) {
+  for (auto& t : tridi::g_tuned)
+    for (int& v : t) v = 0;
+  return TRIDI_SUCCESS;
+}
 
 tridi_status tridi_init(void) { return current_device() ? TRIDI_SUCCESS : TRIDI_ERROR_CUDA; }
 

@@ -31,6 +31,20 @@ inline cudaStream_t as_stream(tridi_stream_t s) { return reinterpret_cast<cudaSt
 // Launch-shape tunables (tridi_set_tunable); 0 means "choose automatically".
 int tunable(int key);
 
+// Table written by the autotuner (tridi_autotune): per table (TRIDI_AUTOTUNE_*)
+// and key (log2 of the system size, or of the size bucket), the chosen value;
+// 0 where nothing was tuned.
+int tuned(int table, int log2key);
+
+inline int ilog2(long v) {
+  int k = 0;
+  while (v > 1) {
+    v >>= 1;
+    ++k;
+  }
+  return k;
+}
+
 // Pipeline depth for a tiled kernel: the tunable if set, else `fallback`,
 // reduced until the shared memory fits the device.
 int pick_stages(size_t fixed_bytes, size_t stage_bytes, int fallback, const DeviceInfo& dev);

@@ -1,27 +1,27 @@
 // Serving loop with continuous batching (no counterpart in the reference).
 //
 // A request is a small ragged batch (host arrays a, b, c, d in FP32, x out
-// in FP64, row offsets).  The scheduler thread
-//   * admits queued requests in arrival order while their HBM footprint fits
-//     the budget and a stream slot is free, coalescing them into one ragged
-//     batch (up to max_batch_rows rows);
-//   * runs each batch on its own stream: stream-ordered cudaMallocAsync, host
-//     -> device copies, an asynchronous plan upload, the refined ragged solve
-//     (FP32 solves, FP64 residual and accumulation, `sweeps` corrections),
-//     device -> pinned-host copies of x and of the residual;
-//   * is told of completion by a host callback on the stream, copies each
-//     request's x out of the pinned buffer, frees the batch's memory
-//     (cudaFreeAsync) and budget, and admits more work.
-// Batches admitted while others are still on the GPU run concurrently on
-// their streams, so new requests do not wait for a whole queue to drain.  A
-// batch whose maximum relative residual misses the tightest tolerance of its
-// requests gets one more correction sweep (up to max_sweeps) before its
-// requests complete.  Each system's arithmetic is independent of what else is
-// in its batch.
+// in FP64, row offsets).  Two kinds of host threads:
+//   * the scheduler admits queued requests in arrival order while their HBM
+//     footprint fits the budget and a stream slot is idle, coalescing them
+//     into one ragged batch (up to max_batch_rows rows), and hands the batch
+//     to that slot;
+//   * each slot's worker runs its batch on the slot's own stream:
+//     stream-ordered cudaMallocAsync, host -> device copies straight from the
+//     callers' arrays, an asynchronous plan upload, the fused refinement
+//     (FP32 solves, extended-precision residual and accumulation, `sweeps`
+//     corrections), the batch's maximum residual read back, one more sweep
+//     while it misses the tightest tolerance of the batch (up to max_sweeps),
+//     then device -> host copies straight into each request's x, the memory
+//     freed (cudaFreeAsync) and the budget returned.
+// Slots work concurrently, so a request that arrives while others are on the
+// GPU is admitted as soon as a slot and memory free up and its work overlaps
+// theirs on the device.  Each system's arithmetic is independent of what else
+// is in its batch.  On a Grace host the copies move pageable memory over the
+// chip-to-chip link directly; no pinned staging buffer is involved.
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -39,6 +39,8 @@ extern "C" tridi_status tridi_ragged_plan_upload_async(const void* plan, void* d
 
 namespace tridi {
 namespace {
+
+constexpr long kMaxServedSystemRows = 24480;  // the ragged solver's largest system
 
 double now_us() {
   return std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -65,27 +67,16 @@ struct Batch {
   std::vector<long> req_row0;  // first row of each request inside the batch
   long rows = 0, systems = 0;
   size_t bytes = 0;
-  int slot = -1;
-  int sweeps = 0;
-  void* plan = nullptr;
-  char* dmem = nullptr;  // one allocation: a, b, c, d, x, workspace, plan, offsets, rel
-  float *da = nullptr, *db = nullptr, *dc = nullptr, *dd = nullptr;
-  double *dx = nullptr, *drel = nullptr;
-  long* doff = nullptr;
-  void *dws = nullptr, *dplan = nullptr;
-  size_t ws_bytes = 0, plan_bytes = 0;
-  std::vector<long> offsets;
 };
 
 class Server;
 
 struct Slot {
-  cudaStream_t stream = nullptr;
-  double* host_x = nullptr;  // pinned staging of x (max_batch_rows)
-  double* host_rel = nullptr;
-  Batch* batch = nullptr;
   Server* server = nullptr;
-  std::atomic<bool> finished{false};
+  cudaStream_t stream = nullptr;
+  double* host_rel = nullptr;  // pinned
+  Batch* batch = nullptr;      // set by the scheduler, cleared when done (under the server mutex)
+  std::thread worker;
 };
 
 class Server {
@@ -103,11 +94,11 @@ class Server {
     for (auto* s : slots_) {
       s->server = this;
       if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-          (e = cudaMallocHost(&s->host_x, sizeof(double) * (size_t)pad4(max_rows_))) != cudaSuccess ||
           (e = cudaMallocHost(&s->host_rel, sizeof(double))) != cudaSuccess)
         return cuda_status(e);
     }
-    thread_ = std::thread([this] { loop(); });
+    for (auto* s : slots_) s->worker = std::thread([this, s] { work(s); });
+    scheduler_ = std::thread([this] { schedule(); });
     return TRIDI_SUCCESS;
   }
 
@@ -117,11 +108,10 @@ class Server {
       stop_ = true;
     }
     cv_.notify_all();
-    if (thread_.joinable()) thread_.join();
+    if (scheduler_.joinable()) scheduler_.join();
+    for (auto* s : slots_)
+      if (s->worker.joinable()) s->worker.join();
     for (auto* s : slots_) {
-      if (s->stream) cudaStreamSynchronize(s->stream);
-      if (s->batch) finish_batch(s, /*failed=*/true);
-      if (s->host_x) cudaFreeHost(s->host_x);
       if (s->host_rel) cudaFreeHost(s->host_rel);
       if (s->stream) cudaStreamDestroy(s->stream);
       delete s;
@@ -147,7 +137,7 @@ class Server {
       return TRIDI_ERROR_INVALID_VALUE;
     }
     for (int s = 0; s < num_systems; ++s)
-      if (offsets[s + 1] <= offsets[s] || offsets[s + 1] - offsets[s] > 17408) {
+      if (offsets[s + 1] <= offsets[s] || offsets[s + 1] - offsets[s] > kMaxServedSystemRows) {
         delete r;
         return TRIDI_ERROR_UNSUPPORTED_SIZE;
       }
@@ -175,9 +165,11 @@ class Server {
     Request* r = it->second;
     const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms);
     while (!r->done) {
-      if (timeout_ms >= 0 && done_cv_.wait_until(l, deadline) == std::cv_status::timeout && !r->done)
-        return TRIDI_ERROR_BUSY;
-      if (timeout_ms < 0) done_cv_.wait(l);
+      if (timeout_ms >= 0) {
+        if (done_cv_.wait_until(l, deadline) == std::cv_status::timeout && !r->done) return TRIDI_ERROR_BUSY;
+      } else {
+        done_cv_.wait(l);
+      }
     }
     if (status) *status = r->status;
     if (sweeps) *sweeps = r->sweeps;
@@ -196,177 +188,163 @@ class Server {
     if (max_inflight_seen) *max_inflight_seen = max_inflight_seen_;
   }
 
-  // called from the stream's host callback thread: no CUDA calls here
-  void notify_finished(Slot* s) {
-    s->finished.store(true);
-    {
-      std::lock_guard<std::mutex> l(mu_);
-      ++pending_completions_;
-    }
-    cv_.notify_all();
-  }
-
  private:
-  void loop() {
-    cudaSetDevice(device_);
+  // ---- scheduler thread ----
+  void schedule() {
     std::unique_lock<std::mutex> l(mu_);
     while (true) {
-      cv_.wait(l, [this] { return stop_ || pending_completions_ > 0 || (!queue_.empty() && free_slot() >= 0); });
+      cv_.wait(l, [this] { return stop_ || (!queue_.empty() && idle_slot() >= 0); });
       if (stop_) return;
-      pending_completions_ = 0;
-      l.unlock();
-      for (auto* s : slots_)
-        if (s->batch && s->finished.exchange(false)) complete(s);
-      l.lock();
-      admit(l);
+      if (!admit()) {
+        // the head request waits for memory: sleep until a batch completes
+        const long long seen = batches_done_;
+        cv_.wait(l, [this, seen] { return stop_ || batches_done_ != seen; });
+      }
     }
   }
 
-  int free_slot() const {
+  int idle_slot() const {
     for (size_t i = 0; i < slots_.size(); ++i)
       if (!slots_[i]->batch) return (int)i;
     return -1;
   }
 
-  // mu_ held on entry and exit
-  void admit(std::unique_lock<std::mutex>& l) {
+  // mu_ held.  Forms one batch for an idle slot; false when the head request
+  // does not fit the memory left.
+  bool admit() {
+    const int si = idle_slot();
+    auto* b = new Batch();
     while (!queue_.empty()) {
-      const int si = free_slot();
-      if (si < 0) return;
-      auto* b = new Batch();
-      while (!queue_.empty()) {
-        Request* r = queue_.front();
-        const long sys = (long)r->offsets.size() - 1;
-        const size_t fp = footprint(b->rows + r->rows, b->systems + sys);
-        if (b->rows + r->rows > max_rows_ || used_ + fp > budget_) break;
-        b->req_row0.push_back(b->rows);
-        b->reqs.push_back(r);
-        b->rows += r->rows;
-        b->systems += sys;
-        queue_.pop_front();
+      Request* r = queue_.front();
+      const long sys = (long)r->offsets.size() - 1;
+      const size_t fp = footprint(b->rows + r->rows, b->systems + sys);
+      if (b->rows + r->rows > max_rows_ || used_ + fp > budget_) break;
+      b->req_row0.push_back(b->rows);
+      b->reqs.push_back(r);
+      b->rows += r->rows;
+      b->systems += sys;
+      queue_.pop_front();
+    }
+    if (b->reqs.empty()) {
+      delete b;
+      return false;
+    }
+    b->bytes = footprint(b->rows, b->systems);
+    used_ += b->bytes;
+    ++batches_;
+    const double t = now_us();
+    for (auto* r : b->reqs) r->t_admit = t;
+    slots_[si]->batch = b;
+    int inflight = 0;
+    for (auto* s : slots_) inflight += s->batch != nullptr;
+    max_inflight_seen_ = std::max(max_inflight_seen_, (double)inflight);
+    cv_.notify_all();  // wakes the slot's worker
+    return true;
+  }
+
+  // ---- slot workers ----
+  void work(Slot* s) {
+    cudaSetDevice(device_);
+    while (true) {
+      Batch* b = nullptr;
+      {
+        std::unique_lock<std::mutex> l(mu_);
+        cv_.wait(l, [this, s] { return stop_ || s->batch != nullptr; });
+        if (!s->batch) return;  // stopping, nothing assigned
+        b = s->batch;
       }
-      if (b->reqs.empty()) {  // the head request waits for memory to free up
-        delete b;
-        return;
-      }
-      b->bytes = footprint(b->rows, b->systems);
-      used_ += b->bytes;
-      b->slot = si;
-      slots_[si]->batch = b;
-      ++batches_;
-      int inflight = 0;
-      for (auto* s : slots_) inflight += s->batch != nullptr;
-      max_inflight_seen_ = std::max(max_inflight_seen_, (double)inflight);
-      const double t = now_us();
-      for (auto* r : b->reqs) r->t_admit = t;
-      l.unlock();
-      const tridi_status st = launch(slots_[si], b, sweeps_);
-      l.lock();
-      if (st != TRIDI_SUCCESS) {
-        for (auto* r : b->reqs) {
-          r->status = st;
-          r->t_done = now_us();
-          r->done = true;
-        }
-        used_ -= b->bytes;
-        slots_[si]->batch = nullptr;
-        release(b);
-        done_cv_.notify_all();
-      }
+      int sweeps = 0;
+      double rel = 0.0;
+      const tridi_status st = run(s, b, &sweeps, &rel);
+      finish(s, b, st, sweeps, rel);
     }
   }
 
-  static void CUDART_CB on_done(void* user) {
-    Slot* s = static_cast<Slot*>(user);
-    s->server->notify_finished(s);
-  }
-
-  tridi_status launch(Slot* s, Batch* b, int sweeps) {
+  // Runs one batch to completion on the slot's stream (this thread blocks on
+  // its own stream only).
+  tridi_status run(Slot* s, Batch* b, int* sweeps_out, double* rel_out) {
     cudaStream_t st = s->stream;
     cudaError_t e;
-    if (!b->dmem) {
-      // concatenated offsets and the plan
-      b->offsets.assign(1, 0);
-      for (auto* r : b->reqs)
-        for (size_t k = 1; k < r->offsets.size(); ++k) b->offsets.push_back(b->offsets.back() + r->offsets[k] - r->offsets[k - 1]);
-      tridi_status ts = tridi_ragged_plan_create(b->offsets.data(), (int)b->systems, &b->plan);
-      if (ts != TRIDI_SUCCESS) return ts;
-      const long R = pad4(b->rows);
-      b->ws_bytes = tridi_ragged_refine_workspace_bytes(b->rows, b->systems);
-      b->plan_bytes = tridi_ragged_plan_device_bytes(b->plan);
-      const size_t sizes[] = {align256(4 * R), align256(4 * R), align256(4 * R), align256(4 * R), align256(8 * R),
-                              align256(b->ws_bytes), align256(b->plan_bytes),
-                              align256(sizeof(long) * (b->systems + 1)), 256};
-      size_t total = 0;
-      for (size_t v : sizes) total += v;
-      if ((e = cudaMallocAsync(reinterpret_cast<void**>(&b->dmem), total, st)) != cudaSuccess) return cuda_status(e);
-      char* p = b->dmem;
-      b->da = reinterpret_cast<float*>(p); p += sizes[0];
-      b->db = reinterpret_cast<float*>(p); p += sizes[1];
-      b->dc = reinterpret_cast<float*>(p); p += sizes[2];
-      b->dd = reinterpret_cast<float*>(p); p += sizes[3];
-      b->dx = reinterpret_cast<double*>(p); p += sizes[4];
-      b->dws = p; p += sizes[5];
-      b->dplan = p; p += sizes[6];
-      b->doff = reinterpret_cast<long*>(p); p += sizes[7];
-      b->drel = reinterpret_cast<double*>(p);
+    std::vector<long> offsets(1, 0);
+    for (auto* r : b->reqs)
+      for (size_t k = 1; k < r->offsets.size(); ++k)
+        offsets.push_back(offsets.back() + r->offsets[k] - r->offsets[k - 1]);
+    void* plan = nullptr;
+    tridi_status ts = tridi_ragged_plan_create(offsets.data(), (int)b->systems, &plan);
+    if (ts != TRIDI_SUCCESS) return ts;
+    const long R = pad4(b->rows);
+    const size_t ws_bytes = tridi_ragged_refine_workspace_bytes(b->rows, b->systems);
+    const size_t plan_bytes = tridi_ragged_plan_device_bytes(plan);
+    const size_t sizes[] = {align256(4 * R), align256(4 * R), align256(4 * R), align256(4 * R),
+                            align256(8 * R), align256(ws_bytes), align256(plan_bytes), 256};
+    size_t total = 0;
+    for (size_t v : sizes) total += v;
+    char* dmem = nullptr;
+    if ((e = cudaMallocAsync(reinterpret_cast<void**>(&dmem), total, st)) != cudaSuccess) {
+      tridi_ragged_plan_destroy(plan);
+      return cuda_status(e);
+    }
+    char* p = dmem;
+    float* da = reinterpret_cast<float*>(p); p += sizes[0];
+    float* db = reinterpret_cast<float*>(p); p += sizes[1];
+    float* dc = reinterpret_cast<float*>(p); p += sizes[2];
+    float* dd = reinterpret_cast<float*>(p); p += sizes[3];
+    double* dx = reinterpret_cast<double*>(p); p += sizes[4];
+    void* dws = p; p += sizes[5];
+    void* dplan = p; p += sizes[6];
+    double* drel = reinterpret_cast<double*>(p);
+    auto body = [&]() -> tridi_status {
       // pad rows of the coefficient arrays are read by the bulk copies: define them
       const size_t tail = (size_t)(R - b->rows) * 4;
-      for (float* arr : {b->da, b->db, b->dc, b->dd})
+      for (float* arr : {da, db, dc, dd})
         if (tail && (e = cudaMemsetAsync(arr + b->rows, 0, tail, st)) != cudaSuccess) return cuda_status(e);
       for (size_t q = 0; q < b->reqs.size(); ++q) {
         Request* r = b->reqs[q];
         const size_t off = (size_t)b->req_row0[q], bytes = (size_t)r->rows * 4;
-        if ((e = cudaMemcpyAsync(b->da + off, r->a, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(b->db + off, r->b, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(b->dc + off, r->c, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(b->dd + off, r->d, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        if ((e = cudaMemcpyAsync(da + off, r->a, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(db + off, r->b, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(dc + off, r->c, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(dd + off, r->d, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
           return cuda_status(e);
       }
-      if ((e = cudaMemcpyAsync(b->doff, b->offsets.data(), sizeof(long) * (b->systems + 1), cudaMemcpyHostToDevice,
-                               st)) != cudaSuccess)
-        return cuda_status(e);
-      ts = tridi_ragged_plan_upload_async(b->plan, b->dplan, b->plan_bytes, st);
-      if (ts != TRIDI_SUCCESS) return ts;
-    }
-    b->sweeps = sweeps;
-    tridi_status ts = tridi_ragged_refine_f32(b->da, b->db, b->dc, b->dd, b->dx, b->plan, b->dplan, b->doff, sweeps,
-                                              b->dws, b->ws_bytes, b->drel, st);
-    if (ts != TRIDI_SUCCESS) return ts;
-    if ((e = cudaMemcpyAsync(s->host_x, b->dx, sizeof(double) * b->rows, cudaMemcpyDeviceToHost, st)) !=
-            cudaSuccess ||
-        (e = cudaMemcpyAsync(s->host_rel, b->drel, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaLaunchHostFunc(st, on_done, s)) != cudaSuccess)
-      return cuda_status(e);
-    return TRIDI_SUCCESS;
+      tridi_status t = tridi_ragged_plan_upload_async(plan, dplan, plan_bytes, st);
+      if (t != TRIDI_SUCCESS) return t;
+      double tol = 1e300;
+      for (auto* r : b->reqs) tol = std::min(tol, r->tol);
+      for (int sweeps = sweeps_;; ++sweeps) {
+        t = tridi_ragged_refine_f32(da, db, dc, dd, dx, plan, dplan, nullptr, sweeps, dws, ws_bytes, drel, st);
+        if (t != TRIDI_SUCCESS) return t;
+        if ((e = cudaMemcpyAsync(s->host_rel, drel, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+          return cuda_status(e);
+        *rel_out = *s->host_rel;
+        *sweeps_out = sweeps;
+        if (*rel_out <= tol || !(*rel_out == *rel_out) || sweeps >= max_sweeps_) break;
+      }
+      for (size_t q = 0; q < b->reqs.size(); ++q) {
+        Request* r = b->reqs[q];
+        if ((e = cudaMemcpyAsync(r->x, dx + b->req_row0[q], sizeof(double) * r->rows, cudaMemcpyDeviceToHost, st)) !=
+            cudaSuccess)
+          return cuda_status(e);
+      }
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_status(e);
+      return TRIDI_SUCCESS;
+    };
+    ts = body();
+    cudaFreeAsync(dmem, st);
+    cudaStreamSynchronize(st);  // the plan's host arrays feed the upload: keep them until it ran
+    tridi_ragged_plan_destroy(plan);
+    return ts;
   }
 
-  // scheduler thread, mu_ not held
-  void complete(Slot* s) {
-    Batch* b = s->batch;
-    const double rel = *s->host_rel;
-    double tol = 1e300;
-    for (auto* r : b->reqs) tol = std::min(tol, r->tol);
-    if (!(rel <= tol) && b->sweeps < max_sweeps_ && rel == rel) {
-      if (launch(s, b, b->sweeps + 1) == TRIDI_SUCCESS) return;  // one more correction sweep
-    }
-    for (size_t q = 0; q < b->reqs.size(); ++q) {
-      Request* r = b->reqs[q];
-      std::memcpy(r->x, s->host_x + b->req_row0[q], sizeof(double) * r->rows);
-      r->rel = rel;
-      r->sweeps = b->sweeps;
-      r->status = rel <= r->tol ? TRIDI_SUCCESS : TRIDI_ERROR_NOT_CONVERGED;
-    }
-    finish_batch(s, false);
-  }
-
-  void finish_batch(Slot* s, bool failed) {
-    Batch* b = s->batch;
+  void finish(Slot* s, Batch* b, tridi_status st, int sweeps, double rel) {
     const double t = now_us();
     {
       std::lock_guard<std::mutex> l(mu_);
       for (auto* r : b->reqs) {
-        if (failed) r->status = TRIDI_ERROR_CUDA;
+        r->rel = rel;
+        r->sweeps = sweeps;
+        r->status = st != TRIDI_SUCCESS ? st : (rel <= r->tol ? TRIDI_SUCCESS : TRIDI_ERROR_NOT_CONVERGED);
         r->t_done = t;
         r->done = true;
         ++completed_;
@@ -374,15 +352,11 @@ class Server {
       }
       used_ -= b->bytes;
       s->batch = nullptr;
+      ++batches_done_;
     }
-    if (b->dmem) cudaFreeAsync(b->dmem, s->stream);
-    release(b);
-    done_cv_.notify_all();
-  }
-
-  void release(Batch* b) {
-    if (b->plan) tridi_ragged_plan_destroy(b->plan);
     delete b;
+    cv_.notify_all();
+    done_cv_.notify_all();
   }
 
   size_t budget_, used_ = 0;
@@ -394,11 +368,10 @@ class Server {
   std::condition_variable cv_, done_cv_;
   std::deque<Request*> queue_;
   std::unordered_map<long long, Request*> all_;
-  long long next_id_ = 0, completed_ = 0, batches_ = 0, rows_done_ = 0;
+  long long next_id_ = 0, completed_ = 0, batches_ = 0, batches_done_ = 0, rows_done_ = 0;
   double max_inflight_seen_ = 0;
-  int pending_completions_ = 0;
   bool stop_ = false;
-  std::thread thread_;
+  std::thread scheduler_;
 };
 
 }  // namespace

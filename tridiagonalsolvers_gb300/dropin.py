@@ -71,3 +71,17 @@ def crNBC32(a, b, c, d, x, system_size, num_systems):
 
 def pcrGaussWrapper(a, b, c, d, x, system_size, num_systems, gaussian):
     return _solve(PCR_THOMAS, a, b, c, d, x, system_size, num_systems, gaussian)
+
+
+def write_result_file(x, num_systems, system_size, path):
+    """The reference driver's text dump of a solution (writeResultToFile,
+    tridiagonal_gold.h:96-107): per system a header line, then one value per
+    line, C++ default stream format.  x: host float32 or float64 array."""
+    x = np.ascontiguousarray(x)
+    if x.size < num_systems * system_size:
+        raise ValueError("x shorter than num_systems * system_size")
+    fn = {np.dtype(np.float32): "tridi_write_result_file_f32",
+          np.dtype(np.float64): "tridi_write_result_file_f64"}.get(x.dtype)
+    if fn is None:
+        raise TypeError("x must be float32 or float64")
+    check(getattr(lib(), fn)(x.ctypes.data, int(num_systems), int(system_size), str(path).encode()), fn)

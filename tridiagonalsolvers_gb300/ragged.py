@@ -65,19 +65,28 @@ class RaggedPlan:
             self._h = None
 
 
+TUNE_RESIDUAL = 4  # TRIDI_TUNE_RESIDUAL
+RESIDUAL_MODES = {"df": 1, "fp64": 2}  # TRIDI_RESIDUAL_DF, TRIDI_RESIDUAL_FP64
+
+
 class RaggedRefiner:
-    """FP32 ragged solves with FP64 residual refinement, a fixed number of
-    correction sweeps, optionally captured once in a CUDA graph and replayed.
+    """Fused mixed-precision refinement of a ragged batch (one launch): FP32
+    solves, residual and update in extended precision -- "df" (double-float,
+    pairs of FP32) or "fp64" (native) -- a fixed number of correction sweeps,
+    optionally captured once in a CUDA graph and replayed.
 
         r = RaggedRefiner(plan, a, b, c, d, sweeps=1, graph=True)
         x64, rel = r.run()       # FP64 solution (padded rows) and max relative residual
     """
 
-    def __init__(self, plan: RaggedPlan, a, b, c, d, sweeps: int = 1, graph: bool = True):
+    def __init__(self, plan: RaggedPlan, a, b, c, d, sweeps: int = 1, graph: bool = True, residual: str = "df"):
         import torch
 
         L = lib()
         check(L.tridi_init(), "tridi_init")  # status word allocated outside any capture
+        if residual not in RESIDUAL_MODES:
+            raise ValueError(f"residual must be one of {sorted(RESIDUAL_MODES)}")
+        self.residual = residual
         self.plan, self.sweeps = plan, int(sweeps)
         self.inputs = (a, b, c, d)
         dev = a.device
@@ -101,11 +110,17 @@ class RaggedRefiner:
         import torch
 
         a, b, c, d = self.inputs
+        L = lib()
         stream = ctypes.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
-        check(lib().tridi_ragged_refine_f32(a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(),
+        prev = L.tridi_get_tunable(TUNE_RESIDUAL)
+        check(L.tridi_set_tunable(TUNE_RESIDUAL, RESIDUAL_MODES[self.residual]), "tridi_set_tunable")
+        try:
+            check(L.tridi_ragged_refine_f32(a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(),
                                             self.x.data_ptr(), self.plan._h, self.plan._dev.data_ptr(),
                                             self.off.data_ptr(), self.sweeps, self.ws.data_ptr(), self._wsb,
                                             self.rel.data_ptr(), stream), "tridi_ragged_refine_f32")
+        finally:
+            L.tridi_set_tunable(TUNE_RESIDUAL, prev)
 
     def launch(self):
         """Enqueue one refined solve (graph replay if captured); no sync."""
