@@ -484,8 +484,13 @@ def run_serve(args):
     pool = [make_request(rng) for _ in range(args.serve_requests)]
     rows = [int(r[4][-1]) for r in pool]
     total = sum(rows)
-    srv = Server(hbm_budget_bytes=48 << 30, max_batch_rows=1 << 24, max_inflight=3, sweeps=args.sweeps,
-                 max_sweeps=args.sweeps + 2)
+    from tridiagonalsolvers_gb300 import _lib
+
+    L = _lib.lib()
+    copy_mode = {"auto": 0, "memcpy": 1, "direct": 2, "staged": 3}[args.server_copy]
+    L.tridi_set_tunable(5, copy_mode)  # TRIDI_TUNE_SERVER_COPY, read when the server is created
+    srv = Server(hbm_budget_bytes=48 << 30, max_batch_rows=1 << 24, max_inflight=args.server_slots,
+                 sweeps=args.sweeps, max_sweeps=args.sweeps + 2)
 
     def serve_once(arrivals):
         """Submits pool[i] at arrivals[i] seconds after the start; returns
@@ -520,6 +525,7 @@ def run_serve(args):
         sweep.append({"offered_frac_of_saturation": frac, "arrivals": "poisson", "rate_req_per_s": frac * req_rate,
                       "unknowns_per_s": total / w, **lat(inf)})
     stats = srv.stats()
+    stats["worker_phase_ms"] = srv.phase_ms()
     srv.close()
 
     # plain FP32 form of the same rows on the same GPU
@@ -567,7 +573,8 @@ def run_serve(args):
         "config": {"workload": f"served request stream, {len(pool)} requests of 1-4096 systems x 64-16384 unknowns "
                                "(log-uniform, dominant or ADI), refined to 1e-10",
                    "total_unknowns": total, "seed": workloads_seed("c5"), "sweeps": args.sweeps,
-                   "server": {"hbm_budget_gb": 48, "max_batch_rows": 1 << 24, "max_inflight": 3}},
+                   "server": {"hbm_budget_gb": 48, "max_batch_rows": 1 << 24, "max_inflight": args.server_slots,
+                              "host_transfer": args.server_copy}},
         "e2e": {"value": sat, "unit": "unknowns/s", "h2d_bytes_per_step": 16 * total / len(pool),
                 "d2h_bytes_per_step": 8 * total / len(pool), "path": "tridi_server_submit / tridi_server_wait"},
         "latency_sweep": sweep,
@@ -601,6 +608,10 @@ def main():
     ap.add_argument("--sweeps", type=int, default=1, help="refinement sweeps of the ragged / serve workloads")
     ap.add_argument("--serve-requests", type=int, default=200, help="requests of the serve workload")
     ap.add_argument("--no-autotune", action="store_true", help="ragged workload: keep the built-in size classes")
+    ap.add_argument("--server-copy", default="auto", choices=["auto", "memcpy", "direct", "staged"],
+                    help="serve workload: host transfer (auto = staged through pinned buffers by host threads; "
+                         "direct = the GPU reads / writes the callers' arrays)")
+    ap.add_argument("--server-slots", type=int, default=4, help="serve workload: concurrent batches")
     ap.add_argument("--large-n", type=int, default=65536, help="system size of the large workload")
     ap.add_argument("--no-refine", action="store_true", help="large workload: plain solve only")
     args = ap.parse_args()

@@ -47,6 +47,7 @@ typedef enum tridi_status {
 
 /* Bits of the per-device status word (tridi_device_status). */
 #define TRIDI_DEVERR_WAIT_TIMEOUT 0x1u /* an mbarrier / flag wait exceeded its limit */
+#define TRIDI_DEVERR_BAD_PLAN 0x2u     /* a ragged work list out of the order the kernel expects */
 
 typedef void *tridi_stream_t; /* cudaStream_t */
 
@@ -69,6 +70,10 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
 #define TRIDI_TUNE_RESIDUAL 4   /* arithmetic of the fused ragged refinement's residual and update: */
 #define TRIDI_RESIDUAL_DF 1     /*   double-float (pairs of FP32, 48-bit significand; the default) */
 #define TRIDI_RESIDUAL_FP64 2   /*   native FP64 */
+#define TRIDI_TUNE_SERVER_COPY 5  /* host<->device transfer of servers created afterwards: */
+#define TRIDI_SERVER_COPY_MEMCPY 1 /*   1 = cudaMemcpyAsync on the callers' arrays; */
+#define TRIDI_SERVER_COPY_DIRECT 2 /*   2 = kernels read / write the callers' arrays (pageable memory access); */
+#define TRIDI_SERVER_COPY_STAGED 3 /*   0 or 3 = pinned double-buffered staging filled by host threads */
 tridi_status tridi_set_tunable(int key, int value);
 int tridi_get_tunable(int key);
 
@@ -225,6 +230,10 @@ tridi_status tridi_server_wait(void *server, long long id, int timeout_ms, int *
                                double *rel_residual, double *latency_us);
 tridi_status tridi_server_stats(void *server, long long *completed, long long *batches, long long *rows,
                                 double *max_inflight_seen);
+/* Host microseconds the slot workers spent per phase, summed over batches:
+   [0] plan build, [1] allocation and host->device copies, [2] refinement up to
+   the residual read-back, [3] device->host copies, [4] release. */
+tridi_status tridi_server_phase_times(void *server, double *us, int n);
 tridi_status tridi_server_destroy(void *server);
 
 /* Mixed-precision iterative refinement: FP32 a, b, c, d in, FP64 x out.

@@ -78,6 +78,7 @@ _SIGS["tridi_server_submit"] = (c_int, [_P, _P, _P, _P, _P, _P, _P, c_int, c_dou
 _SIGS["tridi_server_wait"] = (c_int, [_P, _LL, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_double),
                                       POINTER(c_double)])
 _SIGS["tridi_server_stats"] = (c_int, [_P, POINTER(_LL), POINTER(_LL), POINTER(_LL), POINTER(c_double)])
+_SIGS["tridi_server_phase_times"] = (c_int, [_P, POINTER(c_double), c_int])
 _SIGS["tridi_server_destroy"] = (c_int, [_P])
 _SIGS["tridi_refine_workspace_bytes"] = (c_size_t, [ctypes.c_long, ctypes.c_long, c_int])
 _SIGS["tridi_refine_f32"] = (c_int, [_P, _P, _P, _P, _P, ctypes.c_long, ctypes.c_long, c_int, c_double, c_int, _P,

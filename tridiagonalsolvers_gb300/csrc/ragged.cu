@@ -2,33 +2,39 @@
 // [off[s], off[s+1]) of a, b, c, d, x), solved by ONE persistent launch.
 // No counterpart in the reference (its launchers take one size per call).
 //
-// Work queue.  The host plan (tridi_ragged_plan_*) sorts the systems into
-// size buckets and cuts them into work items, largest first:
-//   MULTI  up to 15 systems of <= 480 rows: one warp per system
-//   MULTI4 up to 3 systems of 481 .. 2400 rows: 160 threads (own named
-//          barrier) per system, three systems at once
-//   SINGLE one system of 2401 .. ~13800 rows: the whole CTA
-//   BIG    one system of up to 24480 rows, read from global memory (no
-//          staging): every thread owns three chunks of up to 17 rows; pass 1
-//          eliminates them and exports their interfaces, the 1440
-//          separators are solved by PCR in shared memory, pass 2 eliminates
-//          again (rows now in L2) and substitutes back
-// One CTA per SM (480 consumer threads + a producer warp).  Items are sorted
-// largest first and CTA b takes items b, b + grid, b + 2 grid, ... (so every
-// CTA gets the same mix of sizes, and no claim has to wait on an atomic).
+// Work queue.  The host plan (tridi_ragged_plan_*) sorts the systems by size
+// and cuts them into work items, largest first:
+//   SINGLE one system solved by the whole CTA (480 threads)
+//   BIG    one system beyond the shared-memory ring (up to 24480 rows), read
+//          from global memory by the whole CTA: every thread owns three
+//          chunks of up to 17 rows; pass 1 eliminates them and exports their
+//          interfaces, the 1440 separators are solved by PCR in shared
+//          memory, pass 2 eliminates again (rows now in L2) and substitutes
+//          back
+//   GROUP  one system solved by a team of 160 threads
+//   MULTI  up to 5 systems, one warp each, solved by a team
+// Which of 32, 160 or 480 threads a system gets is the autotuner's choice
+// for its size bucket (else 32 up to 480 rows, 160 up to 4800, 480 above).
+// CTA-wide items (SINGLE, BIG) come first in the list.  One CTA per SM: 480
+// consumer threads in 3 teams of 5 warps, and a producer warp.  CTA b takes
+// items b, b + grid, b + 2 grid, ... (so every CTA gets the same mix of
+// sizes, and no claim has to wait on an atomic); its consumers work through
+// the CTA-wide items together, then split into the 3 teams, team t taking
+// every third of the remaining items.  Teams overlap one another's loads,
+// separator solves and barriers.
 //
 // Staging.  Shared memory holds a ring of rows (a, b, c, d, and in the
 // refined modes the two words of x): the producer places each item's rows
 // contiguously at the ring's head (wrapping to row 0 when the tail end is too
 // short), copies every system's 16-byte-aligned row range per array with
 // cp.async.bulk, and publishes the item in one of kSlots descriptor slots
-// through that slot's mbarrier.  Consumers take items in order and release
-// each slot when done; the producer reclaims ring rows oldest first.  So up
-// to kSlots items of any size are in flight, and a large item's copy overlaps
-// the solve of the items before it.
+// through that slot's mbarrier.  Consumers release each slot when done; the
+// producer reclaims ring rows oldest first.  So up to kSlots items of any
+// size are in flight, and a large item's copy overlaps the solve of the items
+// before it.
 //
 // Arithmetic: the partition solver of partition.cuh, per warp (MULTI), per
-// group of 160 threads (MULTI4) or per CTA (SINGLE), with the chunk
+// team of 160 threads (GROUP) or per CTA (SINGLE), with the chunk
 // elimination done in place in the ring (no register arrays, so no bound on
 // rows per thread) and the separators solved by PCR in shuffles (warp) or
 // shared memory (group, CTA).
@@ -59,24 +65,29 @@ namespace tridi {
 constexpr int kRagThreads = 480;       // consumer threads per CTA (15 warps; + 1 producer warp = 16 warps,
                                        // 4 per SM sub-partition, so up to 128 registers per thread)
 constexpr int kRagWarps = kRagThreads / 32;
-constexpr int kSlots = 4;              // items in flight (descriptor slots)
-constexpr int kWarpMaxRows = 480;      // MULTI systems: up to 15 rows per lane
-constexpr int kGroup4Threads = 160;    // MULTI4: threads per system (5 warps)
-constexpr int kGroup4MaxRows = 2400;   // MULTI4 systems: up to 15 rows per thread
-constexpr int kMaxItemSystems = kRagWarps;  // 15
+constexpr int kTeams = 3;              // consumer teams (see the file comment)
+constexpr int kTeamWarps = kRagWarps / kTeams;      // 5
+constexpr int kTeamThreads = 32 * kTeamWarps;       // 160
+constexpr int kSlots = 9;              // items in flight (descriptor slots), 3 per team
+constexpr int kWarpMaxRows = 480;      // MULTI systems by default: up to 15 rows per lane
+constexpr int kGroupMaxRows = 4800;    // GROUP systems by default: up to 30 rows per thread
+constexpr int kMaxItemSystems = kTeamWarps;  // 5
+static_assert(kTeams * kTeamWarps == kRagWarps && kSlots % kTeams == 0, "team shape");
 constexpr int kBigChunks = 3;                           // chunks per thread for BIG systems
 constexpr int kBigSepRows = kBigChunks * kRagThreads;   // chunks (separators) of a BIG system
 constexpr int kBigKC = 17;                              // rows per BIG chunk at most
 constexpr int kMaxBigRows = kBigKC * kBigSepRows;       // 24480
 constexpr int kBigScratchRows = 2 * kBigSepRows;        // ring rows a BIG item borrows as scratch
 
-enum ItemKind : int { kMulti = 0, kMulti4 = 1, kSingle = 2, kBig = 3, kEnd = 4 };
+// MULTI and GROUP items are a team's; SINGLE and BIG take the whole CTA.
+enum ItemKind : int { kMulti = 0, kGroup = 1, kSingle = 2, kBig = 3, kEnd = 4 };
 enum RagMode : int { kPlain = 0, kRefineDF = 1, kRefineFP64 = 2 };
 
 // Shared-memory map: [head: 2 x kSlots mbarriers, kSlots descriptors]
 // [group scratch: kGroupFloats] [ring: ring_arrays(M) x ring_rows(M) floats].
 constexpr int kHeadBytes = 1280;
 constexpr int kGroupFloats = 4 * kRagThreads + kRagThreads + 48 + 2 * 2 * kRagWarps;  // R, X, F0, norms
+// (CTA-wide items use all of R, X, F0; team t uses its third of each.)
 constexpr int kSmemBudget = 232448;  // 227 KB, the opt-in maximum of sm_100-class GPUs
 __host__ __device__ constexpr int ring_arrays(int mode) { return mode == kPlain ? 4 : 6; }
 __host__ __device__ constexpr int ring_rows(int mode) {
@@ -369,19 +380,38 @@ __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& s
                                              float* sa, const float* sb, float* sc, float* sd, float* xh, float* xl,
                                              float* R, float* X, float* F0, double* red) {
   const int n = sy.n;
-  const float* ga = p.a + sy.off;
-  const float* gb = p.b + sy.off;
-  const float* gc = p.c + sy.off;
-  const float* gd = p.d + sy.off;
+  const float* __restrict__ ga = p.a + sy.off;
+  const float* __restrict__ gc = p.c + sy.off;
+  const float* __restrict__ gd = p.d + sy.off;
   XStore<MODE> xs{xh, xl};
+  // The residual loops read a, c, d back from L2 (the elimination overwrote
+  // them in the ring; b is still there): kU rows' loads are issued before
+  // any of them is used, so their latencies overlap.
+  constexpr int kU = 4;
   for (int sw = -1; sw < p.sweeps; ++sw) {  // sw = -1: the first solve
     if (sw >= 0) {
       gsync(bar, gt);  // every x_i written, every eliminated row read
-      for (int i = gtid; i < n; i += gt) {
-        const float a = ga[i], b = gb[i], c = gc[i], d = gd[i];
-        sa[i] = a;
-        sc[i] = c;
-        sd[i] = xs.residual(i, n, a, b, c, d);
+      for (int i0 = gtid; i0 < n; i0 += kU * gt) {
+        float av[kU], cv[kU], dv[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int i = i0 + u * gt;
+          if (i < n) {
+            av[u] = __ldg(ga + i);
+            cv[u] = __ldg(gc + i);
+            dv[u] = __ldg(gd + i);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int i = i0 + u * gt;
+          if (i < n) {
+            const float r = xs.residual(i, n, av[u], sb[i], cv[u], dv[u]);
+            sa[i] = av[u];
+            sc[i] = cv[u];
+            sd[i] = r;
+          }
+        }
       }
       gsync(bar, gt);
     }
@@ -391,12 +421,27 @@ __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& s
   gsync(bar, gt);
   float rr = 0.f, dd = 0.f;
   double* xo = p.x64 + sy.off;
-  for (int i = gtid; i < n; i += gt) {
-    const float d = gd[i];
-    const float r = xs.residual(i, n, ga[i], gb[i], gc[i], d);
-    rr = fmaf(r, r, rr);
-    dd = fmaf(d, d, dd);
-    xo[i] = xs.get64(i);
+  for (int i0 = gtid; i0 < n; i0 += kU * gt) {
+    float av[kU], cv[kU], dv[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int i = i0 + u * gt;
+      if (i < n) {
+        av[u] = __ldg(ga + i);
+        cv[u] = __ldg(gc + i);
+        dv[u] = __ldg(gd + i);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int i = i0 + u * gt;
+      if (i < n) {
+        const float r = xs.residual(i, n, av[u], sb[i], cv[u], dv[u]);
+        rr = fmaf(r, r, rr);
+        dd = fmaf(dv[u], dv[u], dd);
+        xo[i] = xs.get64(i);
+      }
+    }
   }
   group_rel_max(rr, dd, gt, bar, gtid, red, p.rel);
 }
@@ -543,6 +588,7 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
     int k = 0;       // items published
     int oldest = 0;  // oldest item not yet reclaimed
     int head = 0;    // next free ring row
+    int ends = 0;    // END markers published: one per team
     RagItem nxt{kEnd, 0, 0, 0};
     if ((int)blockIdx.x < p.nitems) nxt = p.items[blockIdx.x];
     for (int item = blockIdx.x;; item += gridDim.x) {
@@ -618,7 +664,12 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
         else
           mbar_arrive_expect_tx(&full[s], 16u * (uint32_t)need);
       }
-      if (end) break;
+      if (end) {
+        head = place;
+        ++k;
+        if (++ends == kTeams) break;
+        continue;
+      }
       __syncwarp();
       if (mine > 0) {
         const uint32_t bytes = 4u * (uint32_t)mine;
@@ -635,50 +686,28 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
   }
 
   // ---------------- consumers ----------------
+  // Phase 1: the CTA's SINGLE and BIG items (the plan puts them first), all
+  // 15 warps on each.  Phase 2, from the first team item on: team t (warps
+  // 5t .. 5t+4, named barrier 2 + t) takes items k0 + t, k0 + t + 3, ...
+  // and releases each with 3 arrivals per warp, so every slot's empty
+  // barrier still completes after 15.
   float* A = ring;  // the consumers overwrite a, c, d (and, plain, b with x) of a staged item in place
   float* B = ring + RR;
   float* C = ring + 2 * RR;
   float* D = ring + 3 * RR;
   float* XH = ring + 4 * RR;  // refined modes: x words
   float* XL = ring + 5 * RR;
-  for (int k = 0;; ++k) {
+  int k = 0;
+  for (;; ++k) {
     const int s = k % kSlots;
     const bool ok = consumer_sync_and(kRagThreads, mbar_wait(&full[s], (k / kSlots) & 1, p.status));
-    if (!ok) break;
+    if (!ok) return;
     const RagSlot& ds = desc[s];
     const int kind = ds.kind;
-    if (kind == kEnd) break;
-    if (kind == kMulti) {
-      if (warp < ds.count) {
-        const RagSys sy{ds.off[warp], ds.n[warp], 0};
-        const int base = ds.base[warp];
-        if constexpr (MODE == kPlain) {
-          group_solve_plain(sy.n, 32, 0, lane, A + base, B + base, C + base, D + base, nullptr, nullptr, nullptr,
-                            p.x + sy.off);
-        } else {
-          group_refine<MODE>(p, sy, 32, 0, lane, A + base, B + base, C + base, D + base, XH + base, XL + base,
-                             nullptr, nullptr, nullptr, red);
-        }
-      }
-    } else if (kind == kMulti4) {
-      const int g = tid / kGroup4Threads;
-      if (g < ds.count) {
-        const RagSys sy{ds.off[g], ds.n[g], 0};
-        const int base = ds.base[g];
-        const int gtid = tid - g * kGroup4Threads;
-        float* R = Rsh + g * 4 * kGroup4Threads;
-        float* X = Xsh + g * kGroup4Threads;
-        float* F = F0 + g * 3 * (kGroup4Threads / 32);
-        if constexpr (MODE == kPlain) {
-          group_solve_plain(sy.n, kGroup4Threads, 2 + g, gtid, A + base, B + base, C + base, D + base, R, X, F,
-                            p.x + sy.off);
-        } else {
-          group_refine<MODE>(p, sy, kGroup4Threads, 2 + g, gtid, A + base, B + base, C + base, D + base, XH + base,
-                             XL + base, R, X, F, red);
-        }
-      }
-    } else if (kind == kSingle) {
-      const RagSys sy{ds.off[0], ds.n[0], 0};
+    if (kind == kMulti || kind == kGroup) break;  // the team phase starts at item k
+    if (kind == kEnd) return;
+    const RagSys sy{ds.off[0], ds.n[0], 0};
+    if (kind == kSingle) {
       const int base = ds.base[0];
       if constexpr (MODE == kPlain) {
         group_solve_plain(sy.n, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, Rsh, Xsh, F0,
@@ -688,10 +717,9 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
                            Rsh, Xsh, F0, red);
       }
     } else {  // kBig
-      const RagSys sy{ds.off[0], ds.n[0], 0};
       const int rb = ds.rbase;
       float* Ra = A + rb;
-      float* Rb = ring + RR + rb;
+      float* Rb = B + rb;
       float* Rc = C + rb;
       float* Rd = D + rb;
       if constexpr (MODE == kPlain) {
@@ -704,6 +732,46 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
       }
     }
     release_stage(&empty[s]);
+  }
+  const int team = warp / kTeamWarps, tw = warp - team * kTeamWarps;
+  const int ttid = tid - team * kTeamThreads, tbar = 2 + team;
+  float* tR = Rsh + team * 4 * kTeamThreads;
+  float* tX = Xsh + team * kTeamThreads;
+  float* tF = F0 + team * 3 * kTeamWarps;
+  for (k += team;; k += kTeams) {
+    const int s = k % kSlots;
+    const bool ok = named_sync_and(tbar, kTeamThreads, mbar_wait(&full[s], (k / kSlots) & 1, p.status));
+    if (!ok) return;
+    const RagSlot& ds = desc[s];
+    const int kind = ds.kind;
+    if (kind == kEnd) return;
+    if (kind == kMulti) {
+      if (tw < ds.count) {
+        const RagSys sy{ds.off[tw], ds.n[tw], 0};
+        const int base = ds.base[tw];
+        if constexpr (MODE == kPlain) {
+          group_solve_plain(sy.n, 32, 0, lane, A + base, B + base, C + base, D + base, nullptr, nullptr, nullptr,
+                            p.x + sy.off);
+        } else {
+          group_refine<MODE>(p, sy, 32, 0, lane, A + base, B + base, C + base, D + base, XH + base, XL + base,
+                             nullptr, nullptr, nullptr, red);
+        }
+      }
+    } else if (kind == kGroup) {
+      const RagSys sy{ds.off[0], ds.n[0], 0};
+      const int base = ds.base[0];
+      if constexpr (MODE == kPlain) {
+        group_solve_plain(sy.n, kTeamThreads, tbar, ttid, A + base, B + base, C + base, D + base, tR, tX, tF,
+                          p.x + sy.off);
+      } else {
+        group_refine<MODE>(p, sy, kTeamThreads, tbar, ttid, A + base, B + base, C + base, D + base, XH + base,
+                           XL + base, tR, tX, tF, red);
+      }
+    } else {
+      record_error(p.status, TRIDI_DEVERR_BAD_PLAN);  // a CTA-wide item after the team phase began
+      return;
+    }
+    release_stage_n(&empty[s], kTeams);
   }
 }
 
@@ -751,40 +819,47 @@ tridi_status tridi_ragged_plan_create(const long* offsets, int num_systems, void
   plan->sys.reserve(num_systems);
   for (int s : order) plan->sys.push_back(RagSys{offsets[s], (int)(offsets[s + 1] - offsets[s]), 0});
   // threads per system: the autotuned choice for the system's size bucket,
-  // else 32 up to 480 rows, 160 up to 2400, the whole CTA above
+  // else 32 up to 480 rows, 160 up to 4800, the whole CTA above
   auto threads_for = [](long n) {
     const int t = tuned(TRIDI_AUTOTUNE_RAGGED_THREADS, ilog2(n));
-    if (t == 32 || t == kGroup4Threads || t == kRagThreads) return t;
-    return n <= kWarpMaxRows ? 32 : (n <= kGroup4MaxRows ? kGroup4Threads : kRagThreads);
+    if (t == 32 || t == kTeamThreads || t == kRagThreads) return t;
+    return n <= kWarpMaxRows ? 32 : (n <= kGroupMaxRows ? kTeamThreads : kRagThreads);
   };
-  constexpr long kPackCap = ring_rows(kRefineDF);  // a packed item fits the ring of every mode
+  constexpr long kPackCap = ring_rows(kRefineDF);  // a team item fits the ring of every mode
+  std::vector<RagItem> cta_items, team_items;      // CTA-wide items go first (phase 1 of the kernel)
   int i = 0;
   while (i < num_systems) {
     const RagSys& sy = plan->sys[i];
     const long pr = padded_rows(sy.off, sy.n);
     if (pr > kMaxStagedRows) {
-      plan->items.push_back(RagItem{(int)kBig, 1, i, 0});
+      cta_items.push_back(RagItem{(int)kBig, 1, i, 0});
       ++i;
       continue;
     }
     const int th = pr > kPackCap ? kRagThreads : threads_for(sy.n);
     if (th == kRagThreads) {
-      plan->items.push_back(RagItem{(int)kSingle, 1, i, (int)pr});
+      cta_items.push_back(RagItem{(int)kSingle, 1, i, (int)pr});
       ++i;
       continue;
     }
-    RagItem it{th == 32 ? (int)kMulti : (int)kMulti4, 0, i, 0};
-    const int cap = th == 32 ? kMaxItemSystems : kRagThreads / kGroup4Threads;
-    while (i < num_systems && it.count < cap) {
+    if (th == kTeamThreads) {
+      team_items.push_back(RagItem{(int)kGroup, 1, i, (int)pr});
+      ++i;
+      continue;
+    }
+    RagItem it{(int)kMulti, 0, i, 0};
+    while (i < num_systems && it.count < kMaxItemSystems) {
       const RagSys& t = plan->sys[i];
       const long tr = padded_rows(t.off, t.n);
-      if (tr > kPackCap || threads_for(t.n) != th || it.rows + tr > kPackCap) break;
+      if (tr > kPackCap || threads_for(t.n) != 32 || it.rows + tr > kPackCap) break;
       it.rows += (int)tr;
       ++it.count;
       ++i;
     }
-    plan->items.push_back(it);
+    team_items.push_back(it);
   }
+  plan->items = std::move(cta_items);
+  plan->items.insert(plan->items.end(), team_items.begin(), team_items.end());
   *plan_out = plan;
   return TRIDI_SUCCESS;
 }

@@ -7,7 +7,7 @@
 //     into one ragged batch (up to max_batch_rows rows), and hands the batch
 //     to that slot;
 //   * each slot's worker runs its batch on the slot's own stream:
-//     stream-ordered cudaMallocAsync, host -> device copies straight from the
+//     stream-ordered cudaMallocAsync, host -> device transfer straight from the
 //     callers' arrays, an asynchronous plan upload, the fused refinement
 //     (FP32 solves, extended-precision residual and accumulation, `sweeps`
 //     corrections), the batch's maximum residual read back, one more sweep
@@ -17,8 +17,13 @@
 // Slots work concurrently, so a request that arrives while others are on the
 // GPU is admitted as soon as a slot and memory free up and its work overlaps
 // theirs on the device.  Each system's arithmetic is independent of what else
-// is in its batch.  On a Grace host the copies move pageable memory over the
-// chip-to-chip link directly; no pinned staging buffer is involved.
+// is in its batch.  Host transfers (TRIDI_TUNE_SERVER_COPY): by default in
+// chunks of 2^20 rows through two pinned buffers per slot, which a pool of
+// host threads fills from (and empties into) the callers' pageable arrays in
+// parallel while the copy engines move the other buffer; or plain
+// cudaMemcpyAsync on the callers' arrays; or, where the device can access
+// pageable host memory (a Grace host), kernels that read the callers' arrays
+// and write their x directly.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,6 +53,121 @@ double now_us() {
 long pad4(long v) { return (v + 3) & ~3L; }
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
+// Per-request copy job of a batch: the caller's host arrays and the
+// request's first row inside the batch.
+struct CopyJob {
+  const float* src[4];
+  double* dst;
+  long row0;
+  long rows;
+};
+
+// Host -> device: the GPU reads the callers' (pageable) arrays itself over the
+// coherent chip-to-chip link (pageable memory access), one grid row per job.
+__global__ void gather_kernel(const CopyJob* jobs, float* da, float* db, float* dc, float* dd) {
+  const CopyJob j = jobs[blockIdx.y];
+  float* dst[4] = {da + j.row0, db + j.row0, dc + j.row0, dd + j.row0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < j.rows; i += (long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) dst[q][i] = j.src[q][i];
+  }
+}
+
+// Device -> host: x of each request written straight into the caller's array.
+__global__ void scatter_kernel(const CopyJob* jobs, const double* dx) {
+  const CopyJob j = jobs[blockIdx.y];
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < j.rows; i += (long)gridDim.x * blockDim.x)
+    j.dst[i] = dx[j.row0 + i];
+}
+
+// Host threads that copy between the callers' (pageable) arrays and the
+// pinned staging buffers, in pieces, in parallel; the calling thread works
+// through the pieces too.
+class CopyPool {
+ public:
+  struct Seg {
+    void* dst;
+    const void* src;
+    size_t bytes;
+  };
+  explicit CopyPool(int n) {
+    for (int i = 0; i < n; ++i) th_.emplace_back([this] { loop(); });
+  }
+  ~CopyPool() {
+    {
+      std::lock_guard<std::mutex> l(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  void run(const std::vector<Seg>& segs) {
+    constexpr size_t kPiece = 1 << 20;
+    Job job;
+    {
+      std::lock_guard<std::mutex> l(mu_);
+      for (const Seg& g : segs)
+        for (size_t o = 0; o < g.bytes; o += kPiece) {
+          q_.push_back(Piece{static_cast<char*>(g.dst) + o, static_cast<const char*>(g.src) + o,
+                             std::min(kPiece, g.bytes - o), &job});
+          ++job.left;
+        }
+    }
+    cv_.notify_all();
+    while (true) {  // help, then wait for the pieces others took
+      Piece pc{};
+      {
+        std::unique_lock<std::mutex> l(mu_);
+        if (q_.empty() || q_.front().job != &job) {
+          job.cv.wait(l, [&] { return job.left == 0; });
+          return;
+        }
+        pc = q_.front();
+        q_.pop_front();
+      }
+      std::memcpy(pc.dst, pc.src, pc.bytes);
+      finish(pc);
+    }
+  }
+
+ private:
+  struct Job {
+    long left = 0;
+    std::condition_variable cv;
+  };
+  struct Piece {
+    char* dst;
+    const char* src;
+    size_t bytes;
+    Job* job;
+  };
+  void finish(const Piece& pc) {
+    std::lock_guard<std::mutex> l(mu_);
+    if (--pc.job->left == 0) pc.job->cv.notify_all();
+  }
+  void loop() {
+    while (true) {
+      Piece pc{};
+      {
+        std::unique_lock<std::mutex> l(mu_);
+        cv_.wait(l, [this] { return stop_ || !q_.empty(); });
+        if (stop_ && q_.empty()) return;
+        pc = q_.front();
+        q_.pop_front();
+      }
+      std::memcpy(pc.dst, pc.src, pc.bytes);
+      finish(pc);
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::deque<Piece> q_;
+  bool stop_ = false;
+};
+
+constexpr long kStageRows = 1L << 20;  // rows per pinned staging chunk (16 MB in, 8 MB out)
+
 struct Request {
   long long id = 0;
   const float *a = nullptr, *b = nullptr, *c = nullptr, *d = nullptr;
@@ -75,6 +195,9 @@ struct Slot {
   Server* server = nullptr;
   cudaStream_t stream = nullptr;
   double* host_rel = nullptr;  // pinned
+  float* in_stage[2] = {};     // pinned: a, b, c, d of kStageRows rows each
+  double* out_stage[2] = {};   // pinned: x of kStageRows rows
+  cudaEvent_t in_done[2] = {}, out_done[2] = {};
   Batch* batch = nullptr;      // set by the scheduler, cleared when done (under the server mutex)
   std::thread worker;
 };
@@ -97,6 +220,27 @@ class Server {
           (e = cudaMallocHost(&s->host_rel, sizeof(double))) != cudaSuccess)
         return cuda_status(e);
     }
+    int pageable = 0;
+    if ((e = cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device_)) != cudaSuccess)
+      return cuda_status(e);
+    // Direct access is opt-in: callers' freshly allocated pages fault on the
+    // GPU's first touch, which made it slower than the copy engines in
+    // measurement; it pays only for arrays the host has already touched.
+    const int mode = tunable(TRIDI_TUNE_SERVER_COPY);
+    if (mode == TRIDI_SERVER_COPY_DIRECT && !pageable) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+    direct_ = mode == TRIDI_SERVER_COPY_DIRECT;
+    staged_ = mode == 0 || mode == TRIDI_SERVER_COPY_STAGED;
+    if (staged_) {
+      for (auto* s : slots_)
+        for (int k = 0; k < 2; ++k)
+          if ((e = cudaMallocHost(&s->in_stage[k], sizeof(float) * 4 * kStageRows)) != cudaSuccess ||
+              (e = cudaMallocHost(&s->out_stage[k], sizeof(double) * kStageRows)) != cudaSuccess ||
+              (e = cudaEventCreateWithFlags(&s->in_done[k], cudaEventDisableTiming)) != cudaSuccess ||
+              (e = cudaEventCreateWithFlags(&s->out_done[k], cudaEventDisableTiming)) != cudaSuccess)
+            return cuda_status(e);
+      const unsigned hw = std::thread::hardware_concurrency();
+      pool_ = new CopyPool(std::max(2, std::min(8, (int)(hw ? hw / 2 : 4))));
+    }
     for (auto* s : slots_) s->worker = std::thread([this, s] { work(s); });
     scheduler_ = std::thread([this] { schedule(); });
     return TRIDI_SUCCESS;
@@ -111,7 +255,14 @@ class Server {
     if (scheduler_.joinable()) scheduler_.join();
     for (auto* s : slots_)
       if (s->worker.joinable()) s->worker.join();
+    delete pool_;
     for (auto* s : slots_) {
+      for (int k = 0; k < 2; ++k) {
+        if (s->in_stage[k]) cudaFreeHost(s->in_stage[k]);
+        if (s->out_stage[k]) cudaFreeHost(s->out_stage[k]);
+        if (s->in_done[k]) cudaEventDestroy(s->in_done[k]);
+        if (s->out_done[k]) cudaEventDestroy(s->out_done[k]);
+      }
       if (s->host_rel) cudaFreeHost(s->host_rel);
       if (s->stream) cudaStreamDestroy(s->stream);
       delete s;
@@ -178,6 +329,14 @@ class Server {
     all_.erase(it);
     delete r;
     return TRIDI_SUCCESS;
+  }
+
+  // Host microseconds spent by the slot workers, summed over batches, per
+  // phase: plan build, allocation + host->device copies issued, solve (up to
+  // the residual read-back), device->host copies, free.
+  void phase_us(double* out, int n) {
+    std::lock_guard<std::mutex> l(mu_);
+    for (int i = 0; i < n && i < kPhases; ++i) out[i] = phase_us_[i];
   }
 
   void stats(long long* completed, long long* batches, long long* rows, double* max_inflight_seen) {
@@ -265,6 +424,13 @@ class Server {
   tridi_status run(Slot* s, Batch* b, int* sweeps_out, double* rel_out) {
     cudaStream_t st = s->stream;
     cudaError_t e;
+    double ph[kPhases] = {};
+    double t = now_us();
+    auto lap = [&](int k) {
+      const double u = now_us();
+      ph[k] += u - t;
+      t = u;
+    };
     std::vector<long> offsets(1, 0);
     for (auto* r : b->reqs)
       for (size_t k = 1; k < r->offsets.size(); ++k)
@@ -272,11 +438,20 @@ class Server {
     void* plan = nullptr;
     tridi_status ts = tridi_ragged_plan_create(offsets.data(), (int)b->systems, &plan);
     if (ts != TRIDI_SUCCESS) return ts;
+    lap(0);
     const long R = pad4(b->rows);
     const size_t ws_bytes = tridi_ragged_refine_workspace_bytes(b->rows, b->systems);
     const size_t plan_bytes = tridi_ragged_plan_device_bytes(plan);
+    std::vector<CopyJob> jobs(b->reqs.size());
+    long max_rows = 0;
+    for (size_t q = 0; q < b->reqs.size(); ++q) {
+      Request* r = b->reqs[q];
+      jobs[q] = CopyJob{{r->a, r->b, r->c, r->d}, r->x, b->req_row0[q], r->rows};
+      max_rows = std::max(max_rows, r->rows);
+    }
     const size_t sizes[] = {align256(4 * R), align256(4 * R), align256(4 * R), align256(4 * R),
-                            align256(8 * R), align256(ws_bytes), align256(plan_bytes), 256};
+                            align256(8 * R), align256(ws_bytes), align256(plan_bytes), 256,
+                            align256(sizeof(CopyJob) * jobs.size())};
     size_t total = 0;
     for (size_t v : sizes) total += v;
     char* dmem = nullptr;
@@ -292,23 +467,60 @@ class Server {
     double* dx = reinterpret_cast<double*>(p); p += sizes[4];
     void* dws = p; p += sizes[5];
     void* dplan = p; p += sizes[6];
-    double* drel = reinterpret_cast<double*>(p);
+    double* drel = reinterpret_cast<double*>(p); p += sizes[7];
+    CopyJob* djobs = reinterpret_cast<CopyJob*>(p);
+    const dim3 cgrid((unsigned)std::min<long>((max_rows + 255) / 256, 64), (unsigned)jobs.size());
     auto body = [&]() -> tridi_status {
       // pad rows of the coefficient arrays are read by the bulk copies: define them
       const size_t tail = (size_t)(R - b->rows) * 4;
       for (float* arr : {da, db, dc, dd})
         if (tail && (e = cudaMemsetAsync(arr + b->rows, 0, tail, st)) != cudaSuccess) return cuda_status(e);
-      for (size_t q = 0; q < b->reqs.size(); ++q) {
-        Request* r = b->reqs[q];
-        const size_t off = (size_t)b->req_row0[q], bytes = (size_t)r->rows * 4;
-        if ((e = cudaMemcpyAsync(da + off, r->a, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(db + off, r->b, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(dc + off, r->c, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(dd + off, r->d, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      if (direct_) {
+        if ((e = cudaMemcpyAsync(djobs, jobs.data(), sizeof(CopyJob) * jobs.size(), cudaMemcpyHostToDevice, st)) !=
+            cudaSuccess)
           return cuda_status(e);
+        gather_kernel<<<cgrid, 256, 0, st>>>(djobs, da, db, dc, dd);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+      } else if (staged_) {
+        // chunks of kStageRows rows through two pinned buffers: the pool fills
+        // one while the copy engine drains the other
+        std::vector<CopyPool::Seg> segs;
+        for (long r0 = 0, k = 0; r0 < b->rows; r0 += kStageRows, ++k) {
+          const long r1 = std::min(b->rows, r0 + kStageRows);
+          float* buf = s->in_stage[k & 1];
+          if (k >= 2 && (e = cudaEventSynchronize(s->in_done[k & 1])) != cudaSuccess) return cuda_status(e);
+          segs.clear();
+          for (size_t q = 0; q < b->reqs.size(); ++q) {
+            Request* r = b->reqs[q];
+            const long lo = std::max(r0, b->req_row0[q]), hi = std::min(r1, b->req_row0[q] + r->rows);
+            if (lo >= hi) continue;
+            const float* src[4] = {r->a, r->b, r->c, r->d};
+            for (int a = 0; a < 4; ++a)
+              segs.push_back({buf + a * kStageRows + (lo - r0), src[a] + (lo - b->req_row0[q]),
+                              sizeof(float) * (hi - lo)});
+          }
+          pool_->run(segs);
+          float* dst[4] = {da, db, dc, dd};
+          for (int a = 0; a < 4; ++a)
+            if ((e = cudaMemcpyAsync(dst[a] + r0, buf + a * kStageRows, sizeof(float) * (r1 - r0),
+                                     cudaMemcpyHostToDevice, st)) != cudaSuccess)
+              return cuda_status(e);
+          if ((e = cudaEventRecord(s->in_done[k & 1], st)) != cudaSuccess) return cuda_status(e);
+        }
+      } else {
+        for (size_t q = 0; q < b->reqs.size(); ++q) {
+          Request* r = b->reqs[q];
+          const size_t off = (size_t)b->req_row0[q], bytes = (size_t)r->rows * 4;
+          if ((e = cudaMemcpyAsync(da + off, r->a, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+              (e = cudaMemcpyAsync(db + off, r->b, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+              (e = cudaMemcpyAsync(dc + off, r->c, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+              (e = cudaMemcpyAsync(dd + off, r->d, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return cuda_status(e);
+        }
       }
       tridi_status t = tridi_ragged_plan_upload_async(plan, dplan, plan_bytes, st);
       if (t != TRIDI_SUCCESS) return t;
+      lap(1);
       double tol = 1e300;
       for (auto* r : b->reqs) tol = std::min(tol, r->tol);
       for (int sweeps = sweeps_;; ++sweeps) {
@@ -321,19 +533,59 @@ class Server {
         *sweeps_out = sweeps;
         if (*rel_out <= tol || !(*rel_out == *rel_out) || sweeps >= max_sweeps_) break;
       }
-      for (size_t q = 0; q < b->reqs.size(); ++q) {
-        Request* r = b->reqs[q];
-        if ((e = cudaMemcpyAsync(r->x, dx + b->req_row0[q], sizeof(double) * r->rows, cudaMemcpyDeviceToHost, st)) !=
-            cudaSuccess)
-          return cuda_status(e);
+      lap(2);
+      if (direct_) {
+        scatter_kernel<<<cgrid, 256, 0, st>>>(djobs, dx);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+      } else if (staged_) {
+        // chunk k's copy engine transfer overlaps the pool's copy-out of chunk k-1
+        std::vector<CopyPool::Seg> segs;
+        const long nchunks = (b->rows + kStageRows - 1) / kStageRows;
+        auto copy_out = [&](long k) {
+          const long r0 = k * kStageRows, r1 = std::min(b->rows, r0 + kStageRows);
+          const double* buf = s->out_stage[k & 1];
+          segs.clear();
+          for (size_t q = 0; q < b->reqs.size(); ++q) {
+            Request* r = b->reqs[q];
+            const long lo = std::max(r0, b->req_row0[q]), hi = std::min(r1, b->req_row0[q] + r->rows);
+            if (lo < hi) segs.push_back({r->x + (lo - b->req_row0[q]), buf + (lo - r0), sizeof(double) * (hi - lo)});
+          }
+          pool_->run(segs);
+        };
+        for (long k = 0; k < nchunks; ++k) {
+          const long r0 = k * kStageRows, r1 = std::min(b->rows, r0 + kStageRows);
+          if ((e = cudaMemcpyAsync(s->out_stage[k & 1], dx + r0, sizeof(double) * (r1 - r0), cudaMemcpyDeviceToHost,
+                                   st)) != cudaSuccess ||
+              (e = cudaEventRecord(s->out_done[k & 1], st)) != cudaSuccess)
+            return cuda_status(e);
+          if (k >= 1) {
+            if ((e = cudaEventSynchronize(s->out_done[(k - 1) & 1])) != cudaSuccess) return cuda_status(e);
+            copy_out(k - 1);
+          }
+        }
+        if ((e = cudaEventSynchronize(s->out_done[(nchunks - 1) & 1])) != cudaSuccess) return cuda_status(e);
+        copy_out(nchunks - 1);
+      } else {
+        for (size_t q = 0; q < b->reqs.size(); ++q) {
+          Request* r = b->reqs[q];
+          if ((e = cudaMemcpyAsync(r->x, dx + b->req_row0[q], sizeof(double) * r->rows, cudaMemcpyDeviceToHost,
+                                   st)) != cudaSuccess)
+            return cuda_status(e);
+        }
       }
       if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_status(e);
+      lap(3);
       return TRIDI_SUCCESS;
     };
     ts = body();
     cudaFreeAsync(dmem, st);
     cudaStreamSynchronize(st);  // the plan's host arrays feed the upload: keep them until it ran
     tridi_ragged_plan_destroy(plan);
+    lap(4);
+    {
+      std::lock_guard<std::mutex> l(mu_);
+      for (int k = 0; k < kPhases; ++k) phase_us_[k] += ph[k];
+    }
     return ts;
   }
 
@@ -370,6 +622,11 @@ class Server {
   std::unordered_map<long long, Request*> all_;
   long long next_id_ = 0, completed_ = 0, batches_ = 0, batches_done_ = 0, rows_done_ = 0;
   double max_inflight_seen_ = 0;
+  bool direct_ = false;  // the GPU reads and writes the callers' host arrays itself
+  bool staged_ = false;  // pinned double-buffered staging filled by the copy pool
+  CopyPool* pool_ = nullptr;
+  static constexpr int kPhases = 5;
+  double phase_us_[kPhases] = {};
   bool stop_ = false;
   std::thread scheduler_;
 };
@@ -414,6 +671,12 @@ tridi_status tridi_server_stats(void* server, long long* completed, long long* b
                                 double* max_inflight_seen) {
   if (!server) return TRIDI_ERROR_INVALID_VALUE;
   static_cast<tridi::Server*>(server)->stats(completed, batches, rows, max_inflight_seen);
+  return TRIDI_SUCCESS;
+}
+
+tridi_status tridi_server_phase_times(void* server, double* us, int n) {
+  if (!server || !us || n < 0) return TRIDI_ERROR_INVALID_VALUE;
+  static_cast<tridi::Server*>(server)->phase_us(us, n);
   return TRIDI_SUCCESS;
 }
 

@@ -132,6 +132,30 @@ __device__ __forceinline__ void release_stage(uint64_t* bar) {
   }
 }
 
+// Same, the warp's arrive counting `count` arrivals.
+__device__ __forceinline__ void release_stage_n(uint64_t* bar, uint32_t count) {
+  fence_proxy_async_smem();
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0], %1;\n}" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(bar))),
+                 "r"(count)
+                 : "memory");
+  }
+}
+
+// Barrier with an AND reduction of `pred` over `nthreads` threads on named
+// barrier `id`.
+__device__ __forceinline__ bool named_sync_and(int id, int nthreads, bool pred) {
+  uint32_t out;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}"
+      : "=r"(out)
+      : "r"((uint32_t)pred), "r"(id), "r"(nthreads)
+      : "memory");
+  return out != 0;
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(smem_addr(bar))
                : "memory");

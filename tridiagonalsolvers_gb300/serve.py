@@ -57,6 +57,13 @@ class Server:
               "stats")
         return {"completed": c.value, "batches": b.value, "rows": r.value, "max_inflight_seen": mi.value}
 
+    def phase_ms(self):
+        """Milliseconds the slot workers spent per phase, summed over batches."""
+        v = (ctypes.c_double * 5)()
+        check(lib().tridi_server_phase_times(self._h, v, 5), "phase times")
+        names = ("plan", "alloc_h2d", "refine", "d2h", "release")
+        return {k: v[i] / 1e3 for i, k in enumerate(names)}
+
     def close(self):
         if self._h and self._h.value:
             lib().tridi_server_destroy(self._h)
