@@ -251,6 +251,12 @@ tridi_status tridi_refine_f32(const float *a, const float *b, const float *c, co
                               long num_systems, int layout, double tol, int max_sweeps, void *workspace,
                               size_t workspace_bytes, tridi_stream_t stream, int *sweeps, double *rel_residual);
 
+/* Self-check: out[i] = the FP64 value nearest hi[i] + lo[i] for normalised
+   double-float pairs (|lo| <= ulp_float(hi) / 2), computed the way the fused
+   refinement writes its FP64 solution (device arrays of n elements). */
+tridi_status tridi_selfcheck_df_to_double(const float *hi, const float *lo, double *out, long n,
+                                          tridi_stream_t stream);
+
 /* Allocation-free solve (no counterpart in the reference): for callers that
    cannot call cudaMalloc at solve time, e.g. an application whose device
    memory is all owned by its own pool, or a latency-critical loop that must

@@ -148,3 +148,38 @@ def test_ragged_rejects_oversize_systems():
 
     with pytest.raises(_lib.TridiError):
         RaggedPlan(np.array([0, 100, 100 + 24481]))
+
+
+def test_double_float_to_fp64_is_correctly_rounded(cuda):
+    """The refinement's FP64 output assembly (integer fast path + FP64 add
+    fallback) equals numpy's correctly rounded float64(hi) + float64(lo) for
+    normalised pairs, including lo finer than hi's double ulp, hi a power of
+    two with lo of the opposite sign, zeros and subnormal lo."""
+    import ctypes
+
+    import torch
+
+    from tridiagonalsolvers_gb300 import _lib
+
+    rng = np.random.default_rng(5)
+    n = 1 << 20
+    hi = (rng.standard_normal(n) * 10.0 ** rng.integers(-20, 20, n)).astype(np.float32)
+    hi[:4096] = np.float32(2.0) ** rng.integers(-60, 60, 4096)  # powers of two
+    hi[4096:4200] = 0.0
+    # lo within half an ulp of hi, at every scale below it
+    ulp = np.spacing(np.abs(hi)).astype(np.float64)
+    frac = rng.uniform(-0.5, 0.5, n) * 2.0 ** -rng.integers(0, 40, n).astype(np.float64)
+    lo = (frac * ulp).astype(np.float32)
+    lo[::7] = 0.0
+    lo[4200:4300] = np.float32(1e-42)  # subnormal
+    # keep pairs normalised after rounding lo to float
+    bad = np.abs(lo.astype(np.float64)) > 0.5 * ulp
+    lo[bad] = 0.0
+    want = hi.astype(np.float64) + lo.astype(np.float64)
+    th, tl = torch.from_numpy(hi).to(cuda), torch.from_numpy(lo).to(cuda)
+    out = torch.empty(n, dtype=torch.float64, device=cuda)
+    _lib.check(_lib.lib().tridi_selfcheck_df_to_double(th.data_ptr(), tl.data_ptr(), out.data_ptr(), n,
+                                                       ctypes.c_void_p(0)), "selfcheck")
+    got = out.cpu().numpy()
+    mism = np.flatnonzero(got != want)
+    assert mism.size == 0, f"{mism.size} mismatches, first hi={hi[mism[0]]!r} lo={lo[mism[0]]!r}"

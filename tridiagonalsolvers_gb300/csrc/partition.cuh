@@ -109,8 +109,9 @@ struct ChunkSummary {
 // interior rows i < k-1 get (a, c, d) overwritten by (ap, cp, dp), so the
 // back substitution reads them again instead of holding 3k registers.
 template <class T>
-__device__ __forceinline__ void chunk_eliminate_smem(ChunkSummary<T>& cs, int k, bool first, bool last, T* sa,
-                                                     const T* sb, T* sc, T* sd) {
+__device__ __forceinline__ void chunk_eliminate_smem(ChunkSummary<T>& cs, int k, bool first, bool last,
+                                                     T* __restrict__ sa, const T* __restrict__ sb,
+                                                     T* __restrict__ sc, T* __restrict__ sd) {
   T cprev = T(0), aprev = T(0), dprev = T(0);
 #pragma unroll 4
   for (int i = 0; i < k - 1; ++i) {
@@ -153,9 +154,10 @@ __device__ __forceinline__ Row<T> separator_row_s(const ChunkSummary<T>& cs, T n
 
 // Back substitution of a chunk eliminated by chunk_eliminate_smem: emit(i, x_i)
 // for every row i < k of the chunk, last row first.
+// (emit writes to arrays other than sa, sc, sd.)
 template <class T, class Emit>
-__device__ __forceinline__ void chunk_back_smem(int k, T sj, T sl, const T* sa, const T* sc, const T* sd,
-                                                Emit& emit) {
+__device__ __forceinline__ void chunk_back_smem(int k, T sj, T sl, const T* __restrict__ sa,
+                                                const T* __restrict__ sc, const T* __restrict__ sd, Emit& emit) {
   if (k >= 1) emit(k - 1, sj);
   T xn = sj;
 #pragma unroll 4

@@ -86,7 +86,7 @@ enum RagMode : int { kPlain = 0, kRefineDF = 1, kRefineFP64 = 2 };
 // Shared-memory map: [head: 2 x kSlots mbarriers, kSlots descriptors]
 // [group scratch: kGroupFloats] [ring: ring_arrays(M) x ring_rows(M) floats].
 constexpr int kHeadBytes = 1280;
-constexpr int kGroupFloats = 4 * kRagThreads + kRagThreads + 48 + 2 * 2 * kRagWarps;  // R, X, F0, norms
+constexpr int kGroupFloats = 4 * kRagThreads + kRagThreads + 48 + 2 * 2 * kRagWarps + 4;  // R, X, F0, norms, max
 // (CTA-wide items use all of R, X, F0; team t uses its third of each.)
 constexpr int kSmemBudget = 232448;  // 227 KB, the opt-in maximum of sm_100-class GPUs
 __host__ __device__ constexpr int ring_arrays(int mode) { return mode == kPlain ? 4 : 6; }
@@ -175,6 +175,27 @@ __device__ __forceinline__ double f2d_exact(float f) {
   return (double)f;
 }
 
+// The double nearest hi + lo for a normalised double-float pair
+// (|lo| <= ulp_float(hi) / 2), mostly without the FP64 pipe: when lo is a
+// whole number K of hi's double ulps (its lowest set bit no finer than that
+// ulp, i.e. float exponent of lo >= exponent of hi - 29), hi + lo is exactly
+// representable and its bit pattern is hi's plus or minus K (the sum stays in
+// hi's binade, except when hi is a power of two and lo pulls it below: that
+// case, lo finer than the ulp, and non-normal inputs take one FP64 add).
+__device__ __forceinline__ double df_to_double(float hi, float lo) {
+  const unsigned uh = __float_as_uint(hi), ul = __float_as_uint(lo);
+  const int eh = (int)((uh >> 23) & 0xffu), el = (int)((ul >> 23) & 0xffu);
+  if ((ul & 0x7fffffffu) == 0u) return f2d_exact(hi);
+  const int sh = el - eh + 29;  // lo = +-Ml * 2^sh ulps of hi's double
+  const bool opposite = ((uh ^ ul) >> 31) != 0u;
+  if (eh >= 1 && eh <= 254 && el >= 1 && sh >= 0 && !(opposite && (uh & 0x7fffffu) == 0u)) {
+    const long long H = __double_as_longlong(f2d_exact(hi));
+    const long long K = (long long)((ul & 0x7fffffu) | 0x800000u) << sh;
+    return __longlong_as_double(opposite ? H - K : H + K);
+  }
+  return f2d_exact(hi) + f2d_exact(lo);
+}
+
 // Knuth's TwoSum: s + e == a + b exactly.
 __device__ __forceinline__ float two_sum(float a, float b, float& e) {
   const float s = __fadd_rn(a, b);
@@ -200,7 +221,7 @@ struct XStore {
     if constexpr (MODE == kRefineFP64)
       return __hiloint2double(__float_as_int(l[i]), __float_as_int(h[i]));
     else
-      return f2d_exact(h[i]) + f2d_exact(l[i]);
+      return df_to_double(h[i], l[i]);
   }
   __device__ __forceinline__ void set64(int i, double v) {
     h[i] = __int_as_float(__double2loint(v));
@@ -260,7 +281,8 @@ struct XStore {
 };
 
 // Adds (rr, dd) over a solve group, and its leader folds sqrt(rr) / sqrt(dd)
-// into the batch maximum.  red: 2 doubles per warp of the CTA.
+// into the CTA's maximum `rel` (shared memory; the kernel folds it into the
+// batch maximum once at the end).  red: 2 doubles per warp of the CTA.
 __device__ __forceinline__ void group_rel_max(float rr, float dd, int gt, int bar, int gtid, double* red,
                                               unsigned long long* rel) {
   double r2 = rr, d2 = dd;
@@ -284,8 +306,18 @@ __device__ __forceinline__ void group_rel_max(float rr, float dd, int gt, int ba
     }
   }
   if (gtid == 0) {
-    const double v = d2 > 0.0 ? sqrt(r2) / sqrt(d2) : sqrt(r2);
-    atomicMax(rel, (unsigned long long)__double_as_longlong(v));
+    // sqrt(r2 / d2) in FP32 (GB300's FP64 square root and division are slow):
+    // both sums scaled by a power of two that brings d2 near 1 first, so
+    // neither underflows in FP32
+    double v;
+    const int e = ((__double2hiint(d2) >> 20) & 0x7ff) - 1023;
+    if (d2 > 0.0 && e > -1000 && e < 1000) {
+      const double sc = __hiloint2double((1023 - e) << 20, 0);  // 2^-e
+      v = (double)(sqrtf((float)(r2 * sc)) / sqrtf((float)(d2 * sc)));
+    } else {
+      v = d2 > 0.0 ? sqrt(r2) / sqrt(d2) : sqrt(r2);
+    }
+    atomicMax(rel, (unsigned long long)__double_as_longlong(v));  // the CTA's maximum, in shared memory
   }
 }
 
@@ -402,14 +434,19 @@ __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& s
             dv[u] = __ldg(gd + i);
           }
         }
+        float rv[kU];
 #pragma unroll
         for (int u = 0; u < kU; ++u) {
           const int i = i0 + u * gt;
+          if (i < n) rv[u] = xs.residual(i, n, av[u], sb[i], cv[u], dv[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {  // stores after every load of the batch
+          const int i = i0 + u * gt;
           if (i < n) {
-            const float r = xs.residual(i, n, av[u], sb[i], cv[u], dv[u]);
             sa[i] = av[u];
             sc[i] = cv[u];
-            sd[i] = r;
+            sd[i] = rv[u];
           }
         }
       }
@@ -421,10 +458,11 @@ __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& s
   gsync(bar, gt);
   float rr = 0.f, dd = 0.f;
   double* xo = p.x64 + sy.off;
-  for (int i0 = gtid; i0 < n; i0 += kU * gt) {
-    float av[kU], cv[kU], dv[kU];
+  constexpr int kUF = kU;
+  for (int i0 = gtid; i0 < n; i0 += kUF * gt) {
+    float av[kUF], cv[kUF], dv[kUF];
 #pragma unroll
-    for (int u = 0; u < kU; ++u) {
+    for (int u = 0; u < kUF; ++u) {
       const int i = i0 + u * gt;
       if (i < n) {
         av[u] = __ldg(ga + i);
@@ -433,7 +471,7 @@ __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& s
       }
     }
 #pragma unroll
-    for (int u = 0; u < kU; ++u) {
+    for (int u = 0; u < kUF; ++u) {
       const int i = i0 + u * gt;
       if (i < n) {
         const float r = xs.residual(i, n, av[u], sb[i], cv[u], dv[u]);
@@ -443,7 +481,7 @@ __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& s
       }
     }
   }
-  group_rel_max(rr, dd, gt, bar, gtid, red, p.rel);
+  group_rel_max(rr, dd, gt, bar, gtid, red, reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps));
 }
 
 // A BIG system (rows read straight from global memory, right-hand side rhs):
@@ -552,7 +590,7 @@ __device__ __forceinline__ void big_refine(const RagParams& p, const RagSys& sy,
     dd = fmaf(d, d, dd);
     xo[i] = xs.get64(i);
   }
-  group_rel_max(rr, dd, kRagThreads, 1, tid, red, p.rel);
+  group_rel_max(rr, dd, kRagThreads, 1, tid, red, reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps));
   consumer_sync(kRagThreads);
 }
 
@@ -569,6 +607,7 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
   float* Xsh = Rsh + 4 * kRagThreads;                           // their solution
   float* F0 = Xsh + kRagThreads;                                // lane-0 first-row coefficients (3 per warp)
   double* red = reinterpret_cast<double*>(F0 + 48);             // norms: 2 per warp
+  unsigned long long* cta_rel = reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps);  // the CTA's max
   float* ring = Rsh + kGroupFloats;                             // array q at ring + q * RR
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -578,6 +617,7 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
       mbar_init(&empty[s], kRagWarps);
     }
     mbar_fence_init();
+    *cta_rel = 0ull;
   }
   __syncthreads();
 
@@ -591,14 +631,19 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
     int ends = 0;    // END markers published: one per team
     RagItem nxt{kEnd, 0, 0, 0};
     if ((int)blockIdx.x < p.nitems) nxt = p.items[blockIdx.x];
+    // item records and the lanes' system records are loaded one item ahead
+    RagSys nsy{0, 0, 0};
+    if (nxt.kind != kEnd && lane < nxt.count) nsy = p.sys[nxt.first + lane];
     for (int item = blockIdx.x;; item += gridDim.x) {
       const bool end = item >= p.nitems;
       const RagItem it = nxt;
-      if (item + (int)gridDim.x < p.nitems) nxt = p.items[item + gridDim.x];  // next item's record, early
+      const RagSys sy = end ? RagSys{0, 0, 0} : nsy;
+      if (item + (int)gridDim.x < p.nitems) {
+        nxt = p.items[item + gridDim.x];
+        if (lane < nxt.count) nsy = p.sys[nxt.first + lane];
+      }
       int kind = end ? (int)kEnd : it.kind;
       if (kind == kSingle && it.rows > RR) kind = kBig;  // does not fit this mode's ring
-      RagSys sy{0, 0, 0};
-      if (!end && lane < it.count) sy = p.sys[it.first + lane];
       // ring rows of this lane's system and their exclusive prefix over lanes
       const long lo = sy.off & ~3L, hi = (sy.off + sy.n + 3) & ~3L;
       const int mine = (!end && kind != kBig && lane < it.count) ? (int)(hi - lo) : 0;
@@ -697,81 +742,88 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
   float* D = ring + 3 * RR;
   float* XH = ring + 4 * RR;  // refined modes: x words
   float* XL = ring + 5 * RR;
-  int k = 0;
-  for (;; ++k) {
-    const int s = k % kSlots;
-    const bool ok = consumer_sync_and(kRagThreads, mbar_wait(&full[s], (k / kSlots) & 1, p.status));
-    if (!ok) return;
-    const RagSlot& ds = desc[s];
-    const int kind = ds.kind;
-    if (kind == kMulti || kind == kGroup) break;  // the team phase starts at item k
-    if (kind == kEnd) return;
-    const RagSys sy{ds.off[0], ds.n[0], 0};
-    if (kind == kSingle) {
-      const int base = ds.base[0];
-      if constexpr (MODE == kPlain) {
-        group_solve_plain(sy.n, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, Rsh, Xsh, F0,
-                          p.x + sy.off);
-      } else {
-        group_refine<MODE>(p, sy, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, XH + base, XL + base,
-                           Rsh, Xsh, F0, red);
-      }
-    } else {  // kBig
-      const int rb = ds.rbase;
-      float* Ra = A + rb;
-      float* Rb = B + rb;
-      float* Rc = C + rb;
-      float* Rd = D + rb;
-      if constexpr (MODE == kPlain) {
-        EmitStore em{p.x + sy.off};
-        solve_big(sy, p.a + sy.off, p.b + sy.off, p.c + sy.off, p.d + sy.off, tid, Ra, Rb, Rc, Rd,
-                  Ra + kBigSepRows, Rb + kBigSepRows, Rc + kBigSepRows, Rd + kBigSepRows, em);
-      } else {
-        big_refine<MODE>(p, sy, tid, Ra, Rb, Rc, Rd, Ra + kBigSepRows, Rb + kBigSepRows, Rc + kBigSepRows,
-                         Rd + kBigSepRows, red);
-      }
-    }
-    release_stage(&empty[s]);
-  }
-  const int team = warp / kTeamWarps, tw = warp - team * kTeamWarps;
-  const int ttid = tid - team * kTeamThreads, tbar = 2 + team;
-  float* tR = Rsh + team * 4 * kTeamThreads;
-  float* tX = Xsh + team * kTeamThreads;
-  float* tF = F0 + team * 3 * kTeamWarps;
-  for (k += team;; k += kTeams) {
-    const int s = k % kSlots;
-    const bool ok = named_sync_and(tbar, kTeamThreads, mbar_wait(&full[s], (k / kSlots) & 1, p.status));
-    if (!ok) return;
-    const RagSlot& ds = desc[s];
-    const int kind = ds.kind;
-    if (kind == kEnd) return;
-    if (kind == kMulti) {
-      if (tw < ds.count) {
-        const RagSys sy{ds.off[tw], ds.n[tw], 0};
-        const int base = ds.base[tw];
+  auto consume = [&]() {
+    int k = 0;
+    for (;; ++k) {
+      const int s = k % kSlots;
+      const bool ok = consumer_sync_and(kRagThreads, mbar_wait(&full[s], (k / kSlots) & 1, p.status));
+      if (!ok) return;
+      const RagSlot& ds = desc[s];
+      const int kind = ds.kind;
+      if (kind == kMulti || kind == kGroup) break;  // the team phase starts at item k
+      if (kind == kEnd) return;
+      const RagSys sy{ds.off[0], ds.n[0], 0};
+      if (kind == kSingle) {
+        const int base = ds.base[0];
         if constexpr (MODE == kPlain) {
-          group_solve_plain(sy.n, 32, 0, lane, A + base, B + base, C + base, D + base, nullptr, nullptr, nullptr,
+          group_solve_plain(sy.n, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, Rsh, Xsh, F0,
                             p.x + sy.off);
         } else {
-          group_refine<MODE>(p, sy, 32, 0, lane, A + base, B + base, C + base, D + base, XH + base, XL + base,
-                             nullptr, nullptr, nullptr, red);
+          group_refine<MODE>(p, sy, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, XH + base, XL + base,
+                             Rsh, Xsh, F0, red);
+        }
+      } else {  // kBig
+        const int rb = ds.rbase;
+        float* Ra = A + rb;
+        float* Rb = B + rb;
+        float* Rc = C + rb;
+        float* Rd = D + rb;
+        if constexpr (MODE == kPlain) {
+          EmitStore em{p.x + sy.off};
+          solve_big(sy, p.a + sy.off, p.b + sy.off, p.c + sy.off, p.d + sy.off, tid, Ra, Rb, Rc, Rd,
+                    Ra + kBigSepRows, Rb + kBigSepRows, Rc + kBigSepRows, Rd + kBigSepRows, em);
+        } else {
+          big_refine<MODE>(p, sy, tid, Ra, Rb, Rc, Rd, Ra + kBigSepRows, Rb + kBigSepRows, Rc + kBigSepRows,
+                           Rd + kBigSepRows, red);
         }
       }
-    } else if (kind == kGroup) {
-      const RagSys sy{ds.off[0], ds.n[0], 0};
-      const int base = ds.base[0];
-      if constexpr (MODE == kPlain) {
-        group_solve_plain(sy.n, kTeamThreads, tbar, ttid, A + base, B + base, C + base, D + base, tR, tX, tF,
-                          p.x + sy.off);
-      } else {
-        group_refine<MODE>(p, sy, kTeamThreads, tbar, ttid, A + base, B + base, C + base, D + base, XH + base,
-                           XL + base, tR, tX, tF, red);
-      }
-    } else {
-      record_error(p.status, TRIDI_DEVERR_BAD_PLAN);  // a CTA-wide item after the team phase began
-      return;
+      release_stage(&empty[s]);
     }
-    release_stage_n(&empty[s], kTeams);
+    const int team = warp / kTeamWarps, tw = warp - team * kTeamWarps;
+    const int ttid = tid - team * kTeamThreads, tbar = 2 + team;
+    float* tR = Rsh + team * 4 * kTeamThreads;
+    float* tX = Xsh + team * kTeamThreads;
+    float* tF = F0 + team * 3 * kTeamWarps;
+    for (k += team;; k += kTeams) {
+      const int s = k % kSlots;
+      const bool ok = named_sync_and(tbar, kTeamThreads, mbar_wait(&full[s], (k / kSlots) & 1, p.status));
+      if (!ok) return;
+      const RagSlot& ds = desc[s];
+      const int kind = ds.kind;
+      if (kind == kEnd) return;
+      if (kind == kMulti) {
+        if (tw < ds.count) {
+          const RagSys sy{ds.off[tw], ds.n[tw], 0};
+          const int base = ds.base[tw];
+          if constexpr (MODE == kPlain) {
+            group_solve_plain(sy.n, 32, 0, lane, A + base, B + base, C + base, D + base, nullptr, nullptr, nullptr,
+                              p.x + sy.off);
+          } else {
+            group_refine<MODE>(p, sy, 32, 0, lane, A + base, B + base, C + base, D + base, XH + base, XL + base,
+                               nullptr, nullptr, nullptr, red);
+          }
+        }
+      } else if (kind == kGroup) {
+        const RagSys sy{ds.off[0], ds.n[0], 0};
+        const int base = ds.base[0];
+        if constexpr (MODE == kPlain) {
+          group_solve_plain(sy.n, kTeamThreads, tbar, ttid, A + base, B + base, C + base, D + base, tR, tX, tF,
+                            p.x + sy.off);
+        } else {
+          group_refine<MODE>(p, sy, kTeamThreads, tbar, ttid, A + base, B + base, C + base, D + base, XH + base,
+                             XL + base, tR, tX, tF, red);
+        }
+      } else {
+        record_error(p.status, TRIDI_DEVERR_BAD_PLAN);  // a CTA-wide item after the team phase began
+        return;
+      }
+      release_stage_n(&empty[s], kTeams);
+    }
+  };
+  consume();
+  if constexpr (MODE != kPlain) {  // every consumer has left its loop: fold the CTA's maximum in once
+    consumer_sync(kRagThreads);
+    if (tid == 0) atomicMax(p.rel, *cta_rel);
   }
 }
 
@@ -958,6 +1010,25 @@ long a64(long v) { return (v + 63) & ~63L; }
 }  // namespace tridi
 
 extern "C" {
+
+namespace tridi {
+namespace {
+__global__ void df_to_double_kernel(const float* hi, const float* lo, double* out, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = df_to_double(hi[i], lo[i]);
+}
+}  // namespace
+}  // namespace tridi
+
+// Self-check of the double-float -> FP64 assembly used by the refinement's
+// output (device arrays of n elements).
+tridi_status tridi_selfcheck_df_to_double(const float* hi, const float* lo, double* out, long n,
+                                          tridi_stream_t stream) {
+  if (!hi || !lo || !out || n < 0) return TRIDI_ERROR_INVALID_VALUE;
+  if (n == 0) return TRIDI_SUCCESS;
+  tridi::df_to_double_kernel<<<(unsigned)((n + 255) / 256), 256, 0, tridi::as_stream(stream)>>>(hi, lo, out, n);
+  return tridi::cuda_status(cudaGetLastError());
+}
 
 // Solves every system of the plan.  a..d, x: concatenated rows (device,
 // 16-byte aligned, at least round_up(total_rows, 4) elements).  dev_plan: the
