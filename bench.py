@@ -55,18 +55,23 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """dram bytes per launch of the dominant kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "cr_65536x256_ncu.md"
+def profile_value(name: str, key: str):
+    """A figure recorded in a committed ncu summary under profiles/ (None if absent)."""
+    p = ROOT / "profiles" / name
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch:"):
+        if line.startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].strip())
             except ValueError:
                 return None
     return None
+
+
+def profile_traffic():
+    """dram bytes per launch of the headline kernel from the committed ncu summary."""
+    return profile_value("cr_65536x256_ncu.md", "traffic_bytes_per_launch")
 
 
 class ClockSampler:
@@ -456,7 +461,10 @@ def run_ragged(args):
                    "autotuned_threads_per_system": tuned or "built-in rule (--no-autotune)"},
         "roofline": {"bound": "hbm", "achieved": BYTES_PER_UNKNOWN * total / (ms * 1e-3) / 1e9, "peak": peak,
                      "unit": "GB/s", "frac": BYTES_PER_UNKNOWN * total / (ms * 1e-3) / 1e9 / peak,
-                     "peak_source": kind, "traffic": None},
+                     "peak_source": kind,
+                     "traffic": (lambda b: b * total if b else None)(
+                         profile_value("ragged_100000_ncu.md", "traffic_bytes_per_row")),
+                     "traffic_note": "ncu dram bytes per row of a 20000-system capture, scaled to this batch"},
         "refined": refined["df"],
         "refined_fp64": refined["fp64"],
     }
@@ -492,6 +500,12 @@ def run_serve(args):
     srv = Server(hbm_budget_bytes=48 << 30, max_batch_rows=1 << 24, max_inflight=args.server_slots,
                  sweeps=args.sweeps, max_sweeps=args.sweeps + 2)
 
+    # one output buffer per request, allocated and touched once (a serving
+    # loop reuses its result buffers; first-touch page faults stay out of the timing)
+    outs = [np.zeros(r, dtype=np.float64) for r in rows]
+    for o in outs:
+        o.fill(1.0)
+
     def serve_once(arrivals):
         """Submits pool[i] at arrivals[i] seconds after the start; returns
         (wall seconds, per-request info)."""
@@ -501,13 +515,13 @@ def run_serve(args):
             delay = arrivals[i] - (time.perf_counter() - t0)
             if delay > 0:
                 time.sleep(delay)
-            ids[i] = srv.submit(a, b, c, d, off, tol=1e-10)
+            ids[i] = srv.submit(a, b, c, d, off, tol=1e-10, out=outs[i])
         infos = [srv.wait(rid)[1] for rid in ids]
         return time.perf_counter() - t0, infos
 
     # warm up: kernels loaded, pools grown
-    for a, b, c, d, off in pool[:2]:
-        srv.wait(srv.submit(a, b, c, d, off))
+    for (a, b, c, d, off), o in zip(pool[:2], outs[:2]):
+        srv.wait(srv.submit(a, b, c, d, off, out=o))
     wall, infos = serve_once([0.0] * len(pool))
     sat = total / wall
     def lat(infos):
@@ -563,8 +577,24 @@ def run_serve(args):
     for _ in range(5):
         e2e()
     e2e_s = (time.perf_counter() - t0) / 5
+    # the same from the pageable host arrays the server is given (x into a touched float32 array)
+    pg_in = [torch.from_numpy(np.ascontiguousarray(v)) for v in cat]
+    pg_out = torch.ones(total, dtype=torch.float32)
+
+    def e2e_pageable():
+        for h, t in zip(pg_in, dv):
+            t[:total].copy_(h)
+        plan.solve(*dv, x=dx)
+        pg_out.copy_(dx[:total])
+
+    e2e_pageable()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        e2e_pageable()
+    e2e_pg_s = (time.perf_counter() - t0) / 5
     plain_dev = total / (ms_dev * 1e-3)
     plain_e2e = total / e2e_s
+    plain_e2e_pg = total / e2e_pg_s
     del off_all
     line = {
         "metric": METRIC, "value": sat, "unit": "unknowns/s", "n_gpus": 1, "steps": len(pool), "warmup": 2,
@@ -579,8 +609,11 @@ def run_serve(args):
                 "d2h_bytes_per_step": 8 * total / len(pool), "path": "tridi_server_submit / tridi_server_wait"},
         "latency_sweep": sweep,
         "server_stats": stats,
-        "plain_fp32_same_rows": {"device_resident_unknowns_per_s": plain_dev, "e2e_unknowns_per_s": plain_e2e,
-                                 "served_frac_of_plain_e2e": sat / plain_e2e,
+        "plain_fp32_same_rows": {"device_resident_unknowns_per_s": plain_dev,
+                                 "e2e_pinned_unknowns_per_s": plain_e2e,
+                                 "e2e_pageable_unknowns_per_s": plain_e2e_pg,
+                                 "served_frac_of_plain_e2e_pinned": sat / plain_e2e,
+                                 "served_frac_of_plain_e2e_pageable": sat / plain_e2e_pg,
                                  "served_frac_of_plain_device": sat / plain_dev},
     }
     print(json.dumps(line), flush=True)

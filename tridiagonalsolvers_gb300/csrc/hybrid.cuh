@@ -173,11 +173,15 @@ template <class T, int K, int STRIDE>
 __device__ __forceinline__ void pcr_regs_block(const Row<T> (&r)[K], T (&xr)[K], int t, int tps,
                                                const GroupScratch<T>& sc, int ct) {
   constexpr int R = K / STRIDE;
+  // Row j of the intermediate system (thread j / R, slot j % R) is kept at
+  // scratch index (j % R) * tps + j / R: at a fixed slot the threads of a
+  // warp touch consecutive words, whatever the PCR distance.
+  auto at = [tps](int j) { return (j % R) * tps + j / R; };
   Row<T> y[R];
 #pragma unroll
   for (int q = 0; q < R; ++q) {
     y[q] = r[STRIDE * q + STRIDE - 1];
-    sc.put(t * R + q, y[q]);
+    sc.put(q * tps + t, y[q]);
   }
   const int rest = tps * R;
   consumer_sync(ct);
@@ -188,13 +192,13 @@ __device__ __forceinline__ void pcr_regs_block(const Row<T> (&r)[K], T (&xr)[K],
       const int j = t * R + q;
       const int jl = j - dl < 0 ? 0 : j - dl;
       const int jr = j + dl > rest - 1 ? rest - 1 : j + dl;
-      ny[q] = reduce_row(y[q], sc.get(jl), sc.get(jr));
+      ny[q] = reduce_row(y[q], sc.get(at(jl)), sc.get(at(jr)));
     }
     consumer_sync(ct);
 #pragma unroll
     for (int q = 0; q < R; ++q) {
       y[q] = ny[q];
-      sc.put(t * R + q, y[q]);
+      sc.put(q * tps + t, y[q]);
     }
     consumer_sync(ct);
   }
@@ -202,7 +206,8 @@ __device__ __forceinline__ void pcr_regs_block(const Row<T> (&r)[K], T (&xr)[K],
 #pragma unroll
   for (int q = 0; q < R; ++q) {
     const int j = t * R + q;
-    xr[STRIDE * q + STRIDE - 1] = (j < half) ? solve2_upper(y[q], sc.get(j + half)) : solve2_lower(sc.get(j - half), y[q]);
+    xr[STRIDE * q + STRIDE - 1] =
+        (j < half) ? solve2_upper(y[q], sc.get(at(j + half))) : solve2_lower(sc.get(at(j - half)), y[q]);
   }
 }
 

@@ -26,13 +26,20 @@ class Server:
     def footprint(rows: int, num_systems: int) -> int:
         return int(lib().tridi_server_request_footprint(int(rows), int(num_systems)))
 
-    def submit(self, a, b, c, d, offsets, tol: float = 1e-10) -> int:
+    def submit(self, a, b, c, d, offsets, tol: float = 1e-10, out=None) -> int:
+        """Queues one request; `out` (float64, >= offsets[-1] elements, e.g. a
+        reused buffer) receives x, else a new array does."""
         arrs = [np.ascontiguousarray(v, dtype=np.float32) for v in (a, b, c, d)]
         off = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
         rows = int(off[-1])
         if any(v.size < rows for v in arrs):
             raise ValueError("arrays shorter than offsets[-1]")
-        x = np.empty(rows, dtype=np.float64)
+        if out is None:
+            x = np.empty(rows, dtype=np.float64)
+        else:
+            if out.dtype != np.float64 or not out.flags.c_contiguous or out.size < rows:
+                raise ValueError("out must be a contiguous float64 array of >= offsets[-1] elements")
+            x = out
         rid = ctypes.c_longlong(0)
         check(lib().tridi_server_submit(self._h, *(v.ctypes.data for v in arrs), x.ctypes.data, off.ctypes.data,
                                         len(off) - 1, float(tol), ctypes.byref(rid)), "tridi_server_submit")
