@@ -168,12 +168,16 @@ tridi_status tridi_solve_large_f64(const double *a, const double *b, const doubl
         [2^k, 2^(k+1)), k = 0..14: threads per system (32, 160 or 480) that
         ragged plans created afterwards give systems of that bucket; ADI
         systems.
+     TRIDI_AUTOTUNE_CR_ROWS           key n (power of two, 32..4096): rows per
+        thread (4, 8 or 16; threads per system = n / rows) of the FP32
+        cr / pcr / crpcr kernels; diagonally dominant systems, timed on cr.
    tridi_tuned / tridi_set_tuned read and write the table (key as above,
    0 = not tuned: the built-in choice applies), tridi_autotune_reset clears
    it.  Synchronises `stream`; allocates and frees its own sample. */
 #define TRIDI_AUTOTUNE_CRPCR_REST 0
 #define TRIDI_AUTOTUNE_PCR_THOMAS_SPLIT 1
 #define TRIDI_AUTOTUNE_RAGGED_THREADS 2
+#define TRIDI_AUTOTUNE_CR_ROWS 3
 tridi_status tridi_autotune(int table, long key, long sample_unknowns, tridi_stream_t stream, int *chosen,
                             float *best_ms);
 int tridi_tuned(int table, long key);

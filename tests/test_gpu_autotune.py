@@ -77,3 +77,20 @@ def test_table_round_trip(tmp_path, cuda):
     autotune.load(str(p))
     t = autotune.table()
     assert t["ragged"]["64"] == 160 and t["crpcr_rest"]["256"] == 16 and t["pcr_thomas"]["128"] == 8
+
+
+@pytest.mark.parametrize("n", [64, 512])
+def test_tune_cr_rows_then_solve(cuda, n):
+    import torch
+
+    import tridiagonalsolvers_gb300 as tg
+
+    rows, ms = autotune.tune("cr_rows", n, sample_unknowns=1 << 22)
+    assert rows in (4, 8, 16) and ms > 0
+    assert autotune.table()["cr_rows"][str(n)] == rows
+    a, b, c, d = workloads.dominant(96, n, seed=12)
+    t = [torch.from_numpy(v).to(cuda) for v in (a, b, c, d)]
+    for rr in (4, 8, 16):  # every instantiated shape gives a correct CR
+        autotune.set_table({"cr_rows": {str(n): rr}})
+        x = tg.cr(*t).cpu().numpy()
+        assert gold.rel_residual(a, b, c, d, x).max() <= RES_TOL[np.float32], rr

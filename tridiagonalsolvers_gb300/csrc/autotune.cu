@@ -8,6 +8,8 @@
 //   TRIDI_AUTOTUNE_PCR_THOMAS_SPLIT  PCR/Thomas split (Thomas chains g) per n
 //   TRIDI_AUTOTUNE_RAGGED_THREADS    threads per system per size bucket of the
 //                                    ragged work queue (32, 160 or 480)
+//   TRIDI_AUTOTUNE_CR_ROWS           rows per thread of the FP32 CR / PCR /
+//                                    CR-PCR kernels per power-of-two n
 //
 // The choices land in the process-wide table of runtime.cu (tridi_tuned /
 // tridi_set_tuned); the Python layer saves and reloads it as JSON.
@@ -141,6 +143,28 @@ extern "C" tridi_status tridi_autotune(int table, long key, long sample, tridi_s
         best = v;
       }
     }
+  } else if (table == TRIDI_AUTOTUNE_CR_ROWS) {
+    const int n = (int)key;
+    if (!is_pow2(n) || n < 32 || n > 4096) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+    const long m = sample / n > 0 ? sample / n : 1;
+    Sample smp;
+    tridi_status ts = smp.alloc(m * n, st, 0);
+    if (ts != TRIDI_SUCCESS) return ts;
+    const int saved = tuned(table, ilog2(n));
+    for (int rows : {4, 8, 16}) {
+      if (n / rows > 256 || n / rows < 2) continue;
+      tridi_set_tuned(table, key, rows);
+      float ms = 0.f;
+      ts = time_ms([&]() { return tridi_cr_f32(smp.a, smp.b, smp.c, smp.d, smp.x, n, (int)m, stream); }, st, &ms);
+      if (ts == TRIDI_ERROR_UNSUPPORTED_SIZE) continue;
+      if (ts != TRIDI_SUCCESS) break;
+      if (ms < best_t) {
+        best_t = ms;
+        best = rows;
+      }
+    }
+    tridi_set_tuned(table, key, saved);
+    if (ts != TRIDI_SUCCESS && ts != TRIDI_ERROR_UNSUPPORTED_SIZE) return ts;
   } else if (table == TRIDI_AUTOTUNE_RAGGED_THREADS) {
     const int k = ilog2(key);
     const long lo = 1L << k;

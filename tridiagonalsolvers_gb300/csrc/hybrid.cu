@@ -22,12 +22,15 @@ bool choose_shape(int n, Shape* s) {
   int K;
   if (sizeof(T) == 4) {
     if (n > 4096) return false;
-    K = n <= 16 ? n / 2 : (n == 512 || n == 4096 ? 16 : 8);
+    K = n <= 16 ? n / 2 : (n == 4096 ? 16 : 8);
   } else {
     if (n > 2048) return false;
     K = n <= 8 ? n / 2 : (n == 2048 ? 8 : 4);
   }
-  const int tk = tunable(TRIDI_TUNE_CR_ROWS);
+  // rows per thread: the process-wide tunable, else the autotuned choice for
+  // this n (FP32 only), else the rule above
+  int tk = tunable(TRIDI_TUNE_CR_ROWS);
+  if (tk <= 0 && sizeof(T) == 4) tk = tuned(TRIDI_AUTOTUNE_CR_ROWS, ilog2(n));
   if (tk > 0 && is_pow2(tk) && tk <= n / 2 && n / tk <= 256) {
     // only shapes with an instantiated kernel (see solve_hybrid)
     const bool warp = n / tk <= 32;

@@ -437,10 +437,10 @@ __global__ void __launch_bounds__(MAXT, MINB) hybrid_kernel(HybridParams p) {
       if constexpr (!WARP) ok = consumer_sync_and(ct, ok);
       if (!ok) break;
       const T* st = stages + s * stage_elems + (size_t)g * n + (size_t)t * K;
-      load_vec<T, K>(st + 0 * (size_t)G * n, va);
-      load_vec<T, K>(st + 1 * (size_t)G * n, vb);
-      load_vec<T, K>(st + 2 * (size_t)G * n, vc);
-      load_vec<T, K>(st + 3 * (size_t)G * n, vd);
+      load_vec_smem<T, K>(st + 0 * (size_t)G * n, va);
+      load_vec_smem<T, K>(st + 1 * (size_t)G * n, vb);
+      load_vec_smem<T, K>(st + 2 * (size_t)G * n, vc);
+      load_vec_smem<T, K>(st + 3 * (size_t)G * n, vd);
       release_stage(&empty[s]);
     } else {
       const long base = sys * n + (long)t * K;

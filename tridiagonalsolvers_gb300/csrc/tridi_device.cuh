@@ -231,6 +231,35 @@ __device__ __forceinline__ void load_vec(const T* p, T (&v)[K]) {
     for (int q = 0; q < K; ++q) v[q] = p[q];
   }
 }
+
+// load_vec from shared memory for threads whose K-element slices are
+// consecutive (thread t at p = base + t*K): a 16-byte load of 8 threads is one
+// shared-memory phase, and with slices 32 or 64 bytes apart their first
+// chunks fall on the same banks (2- or 4-way conflicts).  Each thread
+// starts at a different chunk of its slice, (q + t*Q/8) mod Q for Q chunks,
+// so the 8 threads of a phase cover 8 distinct 16-byte bank groups.
+template <class T, int K>
+__device__ __forceinline__ void load_vec_smem(const T* p, T (&v)[K]) {
+  constexpr int Q = (int)(K * sizeof(T) / 16);
+  if constexpr (sizeof(T) == 4 && (K * sizeof(T)) % 16 == 0 && (Q == 2 || Q == 4)) {
+    const int r = (int)((threadIdx.x * Q / 8) % Q);
+    float4 f[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[q] = reinterpret_cast<const float4*>(p)[(q + r) % Q];
+    // chunk j is f[(j - r) mod Q]
+#pragma unroll
+    for (int j = 0; j < Q; ++j) {
+      float4 g = f[0];
+#pragma unroll
+      for (int q = 1; q < Q; ++q)
+        if ((j - r + Q) % Q == q) g = f[q];
+      v[4 * j + 0] = g.x; v[4 * j + 1] = g.y; v[4 * j + 2] = g.z; v[4 * j + 3] = g.w;
+    }
+  } else {
+    load_vec<T, K>(p, v);
+  }
+}
+
 template <class T, int K>
 __device__ __forceinline__ void store_vec(T* p, const T (&v)[K]) {
   if constexpr ((K * sizeof(T)) % 16 == 0) {
