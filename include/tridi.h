@@ -67,7 +67,7 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
 #define TRIDI_TUNE_STAGES 1     /* cp.async.bulk pipeline stages per CTA (1..8) */
 #define TRIDI_TUNE_CRPCR_REST 2 /* switch level of the CR-PCR correction solves */
 #define TRIDI_TUNE_CR_ROWS 3    /* rows per thread of the CR/PCR/CR-PCR kernels (2, 4, 8, 16) */
-#define TRIDI_TUNE_RESIDUAL 4   /* arithmetic of the fused ragged refinement's residual and update: */
+#define TRIDI_TUNE_RESIDUAL 4   /* arithmetic of the refinements' residual and update: */
 #define TRIDI_RESIDUAL_DF 1     /*   double-float (pairs of FP32, 48-bit significand; the default) */
 #define TRIDI_RESIDUAL_FP64 2   /*   native FP64 */
 #define TRIDI_TUNE_SERVER_COPY 5  /* host<->device transfer of servers created afterwards: */
@@ -241,7 +241,8 @@ tridi_status tridi_server_phase_times(void *server, double *us, int n);
 tridi_status tridi_server_destroy(void *server);
 
 /* Mixed-precision iterative refinement: FP32 a, b, c, d in, FP64 x out.
-   Only the residual r = d - T x and the accumulation x += e run in FP64;
+   Only the residual r = d - T x and the accumulation x += e run in extended
+   precision (TRIDI_TUNE_RESIDUAL: double-float by default, native FP64);
    every solve (the first and each correction) is an FP32 solve: CR-PCR for
    power-of-two contiguous n <= 4096, the partition solver for other
    contiguous n <= 8704, the large-system solver otherwise.  Stops when

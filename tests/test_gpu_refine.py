@@ -1,7 +1,8 @@
-"""GPU parity of FP64-residual iterative refinement (tridi_refine_f32) against
-the FP64 oracle: the refined FP64 solution must reach a relative residual of
-1e-10 (the stated target) and agree with the oracle's FP64 solution; the
-number of correction sweeps is recorded."""
+"""GPU parity of mixed-precision iterative refinement (tridi_refine_f32, the
+residual and update in double-float or native FP64) against the FP64 oracle:
+the refined FP64 solution must reach a relative residual of 1e-10 (the stated
+target) and agree with the oracle's FP64 solution; the number of correction
+sweeps is recorded."""
 import numpy as np
 import pytest
 
@@ -29,18 +30,21 @@ def _check(a, b, c, d, x, layout, sweeps, rel):
     print(f"sweeps={sweeps} residual={res.max():.2e} fwd={fwd:.2e}")
 
 
+@pytest.mark.parametrize("residual", ["df", "fp64"])
 @pytest.mark.parametrize("n,m", [(256, 64), (512, 33), (1000, 17), (4096, 8), (20000, 2)])
-def test_refine_contiguous_dominant(cuda, n, m):
+def test_refine_contiguous_dominant(cuda, n, m, residual):
     a, b, c, d = workloads.dominant(m, n, seed=n + m)
-    x, sweeps, rel = tg.refine(*_dev(cuda, a, b, c, d), n, m, tol=TOL)
+    x, sweeps, rel = tg.refine(*_dev(cuda, a, b, c, d), n, m, tol=TOL, residual=residual)
     _check(a, b, c, d, x.cpu().numpy().reshape(m, n), 0, sweeps, rel)
     assert 1 <= sweeps <= 4
 
 
+@pytest.mark.parametrize("residual", ["df", "fp64"])
 @pytest.mark.parametrize("n,m", [(1024, 64), (8192, 96)])
-def test_refine_interleaved_weak(cuda, n, m):
+def test_refine_interleaved_weak(cuda, n, m, residual):
     a, b, c, d = workloads.weak(m, n, seed=1003 + n, layout=1)
-    x, sweeps, rel = tg.refine(*_dev(cuda, a, b, c, d), n, m, layout="interleaved", tol=TOL, max_sweeps=20)
+    x, sweeps, rel = tg.refine(*_dev(cuda, a, b, c, d), n, m, layout="interleaved", tol=TOL, max_sweeps=20,
+                               residual=residual)
     _check(a, b, c, d, x.cpu().numpy().reshape(n, m), 1, sweeps, rel)
 
 
@@ -60,14 +64,16 @@ def test_refine_reports_non_convergence(cuda):
     assert ei.value.status == 6
 
 
-def test_refine_full_size_1024x65536_interleaved(cuda):
+@pytest.mark.parametrize("residual", ["df", "fp64"])
+def test_refine_full_size_1024x65536_interleaved(cuda, residual):
     """The large-system workload with refinement to 1e-10: sampled systems are
     checked against the FP64 oracle."""
     import torch
 
     n, m = 65536, 1024
     a, b, c, d = workloads.weak(m, n, seed=workloads.SEEDS["c3"], layout=1)
-    x, sweeps, rel = tg.refine(*_dev(cuda, a, b, c, d), n, m, layout="interleaved", tol=TOL, max_sweeps=20)
+    x, sweeps, rel = tg.refine(*_dev(cuda, a, b, c, d), n, m, layout="interleaved", tol=TOL, max_sweeps=20,
+                               residual=residual)
     assert bool(torch.isfinite(x).all())
     cols = np.array([0, 5, 500, 1023])
     xs = x.view(n, m)[:, cols].cpu().numpy()

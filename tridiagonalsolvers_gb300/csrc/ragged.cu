@@ -57,6 +57,7 @@
 #include <cstring>
 #include <vector>
 
+#include "dfloat.cuh"
 #include "partition.cuh"
 #include "runtime.h"
 
@@ -141,7 +142,8 @@ struct RagSlot {  // descriptor of an item in flight, written by the producer wa
   int rbase;  // first ring row of the item
   int rrows;  // ring rows it holds
 };
-static_assert(2 * kSlots * 8 + kSlots * sizeof(RagSlot) <= kHeadBytes, "head fits");
+constexpr int kRestageBars = kRagWarps + kTeams + 1;  // one per warp, per team, and the CTA's
+static_assert(2 * kSlots * 8 + kSlots * sizeof(RagSlot) + 8 * kRestageBars <= kHeadBytes, "head fits");
 
 __device__ __forceinline__ int odd_ceil_dev(int v) { return (v & 1) ? v : v + 1; }
 
@@ -160,55 +162,6 @@ __device__ __forceinline__ void gsync(int bar, int gt) {
 
 // ---------------------------------------------------------------------------
 // Extended-precision helpers of the refined modes.
-
-// Exact float -> double by assembling the IEEE-754 fields (normal numbers and
-// zeros; subnormals, infinities and NaNs take the conversion instruction).
-// Keeps the residual's conversions off the FP64 pipe.
-__device__ __forceinline__ double f2d_exact(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xffu;
-  if (e - 1u < 254u) {
-    const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
-    return __hiloint2double((int)hi, (int)(u << 29));
-  }
-  if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-  return (double)f;
-}
-
-// The double nearest hi + lo for a normalised double-float pair
-// (|lo| <= ulp_float(hi) / 2), mostly without the FP64 pipe: when lo is a
-// whole number K of hi's double ulps (its lowest set bit no finer than that
-// ulp, i.e. float exponent of lo >= exponent of hi - 29), hi + lo is exactly
-// representable and its bit pattern is hi's plus or minus K (the sum stays in
-// hi's binade, except when hi is a power of two and lo pulls it below: that
-// case, lo finer than the ulp, and non-normal inputs take one FP64 add).
-__device__ __forceinline__ double df_to_double(float hi, float lo) {
-  const unsigned uh = __float_as_uint(hi), ul = __float_as_uint(lo);
-  const int eh = (int)((uh >> 23) & 0xffu), el = (int)((ul >> 23) & 0xffu);
-  if ((ul & 0x7fffffffu) == 0u) return f2d_exact(hi);
-  const int sh = el - eh + 29;  // lo = +-Ml * 2^sh ulps of hi's double
-  const bool opposite = ((uh ^ ul) >> 31) != 0u;
-  if (eh >= 1 && eh <= 254 && el >= 1 && sh >= 0 && !(opposite && (uh & 0x7fffffu) == 0u)) {
-    const long long H = __double_as_longlong(f2d_exact(hi));
-    const long long K = (long long)((ul & 0x7fffffu) | 0x800000u) << sh;
-    return __longlong_as_double(opposite ? H - K : H + K);
-  }
-  return f2d_exact(hi) + f2d_exact(lo);
-}
-
-// Knuth's TwoSum: s + e == a + b exactly.
-__device__ __forceinline__ float two_sum(float a, float b, float& e) {
-  const float s = __fadd_rn(a, b);
-  const float bb = __fsub_rn(s, a);
-  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-  return s;
-}
-// Dekker's FastTwoSum (|a| >= |b| or a == 0).
-__device__ __forceinline__ float fast_two_sum(float a, float b, float& e) {
-  const float s = __fadd_rn(a, b);
-  e = __fsub_rn(b, __fsub_rn(s, a));
-  return s;
-}
 
 // x_i of the refined modes lives in two float words per row:
 //   RES_DF:   (hi, lo), x = hi + lo, |lo| <= ulp(hi) / 2
@@ -241,11 +194,9 @@ struct XStore {
     if constexpr (MODE == kRefineFP64) {
       set64(i, get64(i) + f2d_exact(v));
     } else {
-      float e;
-      const float s = two_sum(h[i], v, e);
-      float lo;
-      h[i] = fast_two_sum(s, __fadd_rn(e, l[i]), lo);
-      l[i] = lo;
+      const float2 x = df_add(make_float2(h[i], l[i]), v);
+      h[i] = x.x;
+      l[i] = x.y;
     }
   }
   // r_i = d - a x_{i-1} - b x_i - c x_{i+1}, rounded to float (a = 0 at
@@ -257,25 +208,9 @@ struct XStore {
       if (i < n - 1) r = fma(-f2d_exact(c), get64(i + 1), r);
       return (float)r;
     } else {
-      // products of the high words exactly (TwoProd), summed with TwoSum;
-      // the low words' products and all rounding errors go to t
-      const float hm = i > 0 ? h[i - 1] : 0.f, lm = i > 0 ? l[i - 1] : 0.f;
-      const float hp = i < n - 1 ? h[i + 1] : 0.f, lp = i < n - 1 ? l[i + 1] : 0.f;
-      const float am = i > 0 ? a : 0.f, cp = i < n - 1 ? c : 0.f;
-      const float h0 = h[i], l0 = l[i];
-      const float pb = __fmul_rn(b, h0), pa = __fmul_rn(am, hm), pc = __fmul_rn(cp, hp);
-      float t = -(fmaf(b, h0, -pb) + fmaf(am, hm, -pa) + fmaf(cp, hp, -pc));
-      float e;
-      float s = two_sum(d, -pb, e);
-      t += e;
-      s = two_sum(s, -pa, e);
-      t += e;
-      s = two_sum(s, -pc, e);
-      t += e;
-      t = fmaf(-b, l0, t);
-      t = fmaf(-am, lm, t);
-      t = fmaf(-cp, lp, t);
-      return __fadd_rn(s, t);
+      const float2 xm = i > 0 ? make_float2(h[i - 1], l[i - 1]) : make_float2(0.f, 0.f);
+      const float2 xp = i < n - 1 ? make_float2(h[i + 1], l[i + 1]) : make_float2(0.f, 0.f);
+      return df_residual(i > 0 ? a : 0.f, b, i < n - 1 ? c : 0.f, d, xm, make_float2(h[i], l[i]), xp);
     }
   }
 };
@@ -405,81 +340,74 @@ struct EmitX {
   }
 };
 
+// The refinement's re-staging of a system's original a, c, d into its ring
+// slots (the FP32 elimination overwrote them there; b and the x words are
+// untouched): a bulk copy per array on the group's own mbarrier `mb`, whose
+// phase parity is bit `pbit` of `par`.  Every thread of the group orders its
+// earlier ring accesses before the copy (proxy fence + group barrier); the
+// leader issues; all wait (bounded).
+struct Restage {
+  uint64_t* mb;
+  int pbit;
+  float* dst_a;  // ring slot of the system's first padded row, per array
+  float* dst_c;
+  float* dst_d;
+  const float* src_a;  // the same rows in global memory (16-byte aligned)
+  const float* src_c;
+  const float* src_d;
+  uint32_t bytes;
+};
+
+__device__ __forceinline__ void restage(const Restage& rs, uint32_t& par, int gt, int bar, int gtid,
+                                        unsigned* status) {
+  fence_proxy_async_smem();
+  gsync(bar, gt);
+  if (gtid == 0) {
+    mbar_arrive_expect_tx(rs.mb, 3u * rs.bytes);
+    bulk_g2s(rs.dst_a, rs.src_a, rs.bytes, rs.mb);
+    bulk_g2s(rs.dst_c, rs.src_c, rs.bytes, rs.mb);
+    bulk_g2s(rs.dst_d, rs.src_d, rs.bytes, rs.mb);
+  }
+  mbar_wait(rs.mb, (par >> rs.pbit) & 1u, status);
+  par ^= 1u << rs.pbit;
+}
+
 // Refinement of one staged system by its solve group (see the file comment).
 // sa..sd: the system's rows in the ring, xh / xl: its x words in the ring.
+// Before each residual pass the originals are re-staged into the ring, so
+// the passes read shared memory only.
 template <int MODE>
 __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& sy, int gt, int bar, int gtid,
                                              float* sa, const float* sb, float* sc, float* sd, float* xh, float* xl,
-                                             float* R, float* X, float* F0, double* red) {
+                                             float* R, float* X, float* F0, double* red, uint64_t* mb, int pbit,
+                                             uint32_t& par) {
   const int n = sy.n;
-  const float* __restrict__ ga = p.a + sy.off;
-  const float* __restrict__ gc = p.c + sy.off;
-  const float* __restrict__ gd = p.d + sy.off;
   XStore<MODE> xs{xh, xl};
-  // The residual loops read a, c, d back from L2 (the elimination overwrote
-  // them in the ring; b is still there): kU rows' loads are issued before
-  // any of them is used, so their latencies overlap.
-  constexpr int kU = 4;
+  const long lo = sy.off & ~3L, hi = (sy.off + n + 3) & ~3L;
+  const int pad = (int)(sy.off - lo);
+  const Restage rs{mb, pbit, sa - pad, sc - pad, sd - pad, p.a + lo, p.c + lo, p.d + lo,
+                   (uint32_t)(4 * (hi - lo))};
   for (int sw = -1; sw < p.sweeps; ++sw) {  // sw = -1: the first solve
     if (sw >= 0) {
-      gsync(bar, gt);  // every x_i written, every eliminated row read
-      for (int i0 = gtid; i0 < n; i0 += kU * gt) {
-        float av[kU], cv[kU], dv[kU];
-#pragma unroll
-        for (int u = 0; u < kU; ++u) {
-          const int i = i0 + u * gt;
-          if (i < n) {
-            av[u] = __ldg(ga + i);
-            cv[u] = __ldg(gc + i);
-            dv[u] = __ldg(gd + i);
-          }
-        }
-        float rv[kU];
-#pragma unroll
-        for (int u = 0; u < kU; ++u) {
-          const int i = i0 + u * gt;
-          if (i < n) rv[u] = xs.residual(i, n, av[u], sb[i], cv[u], dv[u]);
-        }
-#pragma unroll
-        for (int u = 0; u < kU; ++u) {  // stores after every load of the batch
-          const int i = i0 + u * gt;
-          if (i < n) {
-            sa[i] = av[u];
-            sc[i] = cv[u];
-            sd[i] = rv[u];
-          }
-        }
+      restage(rs, par, gt, bar, gtid, p.status);
+      for (int i = gtid; i < n; i += gt) {  // r overwrites d row by row; a, c stay for the solve
+        const float r = xs.residual(i, n, sa[i], sb[i], sc[i], sd[i]);
+        sd[i] = r;
       }
       gsync(bar, gt);
     }
     EmitX<MODE> em{xs, sw < 0};
     group_solve(n, gt, bar, gtid, sa, sb, sc, sd, R, X, F0, em);
   }
-  gsync(bar, gt);
+  restage(rs, par, gt, bar, gtid, p.status);
   float rr = 0.f, dd = 0.f;
   double* xo = p.x64 + sy.off;
-  constexpr int kUF = kU;
-  for (int i0 = gtid; i0 < n; i0 += kUF * gt) {
-    float av[kUF], cv[kUF], dv[kUF];
-#pragma unroll
-    for (int u = 0; u < kUF; ++u) {
-      const int i = i0 + u * gt;
-      if (i < n) {
-        av[u] = __ldg(ga + i);
-        cv[u] = __ldg(gc + i);
-        dv[u] = __ldg(gd + i);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < kUF; ++u) {
-      const int i = i0 + u * gt;
-      if (i < n) {
-        const float r = xs.residual(i, n, av[u], sb[i], cv[u], dv[u]);
-        rr = fmaf(r, r, rr);
-        dd = fmaf(dv[u], dv[u], dd);
-        xo[i] = xs.get64(i);
-      }
-    }
+  for (int i = gtid; i < n; i += gt) {
+    const float d = sd[i];
+    const float r = xs.residual(i, n, sa[i], sb[i], sc[i], d);
+    rr = fmaf(r, r, rr);
+    dd = fmaf(d, d, dd);
+    xo[i] = xs.get64(i);
   }
   group_rel_max(rr, dd, gt, bar, gtid, red, reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps));
 }
@@ -603,6 +531,7 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + kSlots;
   RagSlot* desc = reinterpret_cast<RagSlot*>(smem + 2 * kSlots * 8);
+  uint64_t* rbar = reinterpret_cast<uint64_t*>(smem + 2 * kSlots * 8 + kSlots * sizeof(RagSlot));  // restaging
   float* Rsh = reinterpret_cast<float*>(smem + kHeadBytes);  // group / CTA separators: 4 x kRagThreads
   float* Xsh = Rsh + 4 * kRagThreads;                           // their solution
   float* F0 = Xsh + kRagThreads;                                // lane-0 first-row coefficients (3 per warp)
@@ -616,6 +545,7 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], kRagWarps);
     }
+    for (int q = 0; q < kRestageBars; ++q) mbar_init(&rbar[q], 1);
     mbar_fence_init();
     *cta_rel = 0ull;
   }
@@ -742,6 +672,7 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
   float* D = ring + 3 * RR;
   float* XH = ring + 4 * RR;  // refined modes: x words
   float* XL = ring + 5 * RR;
+  uint32_t rpar = 0;  // phase parities of the restaging barriers this thread uses
   auto consume = [&]() {
     int k = 0;
     for (;; ++k) {
@@ -760,7 +691,7 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
                             p.x + sy.off);
         } else {
           group_refine<MODE>(p, sy, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, XH + base, XL + base,
-                             Rsh, Xsh, F0, red);
+                             Rsh, Xsh, F0, red, &rbar[kRagWarps + kTeams], kRagWarps + kTeams, rpar);
         }
       } else {  // kBig
         const int rb = ds.rbase;
@@ -800,7 +731,7 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
                               p.x + sy.off);
           } else {
             group_refine<MODE>(p, sy, 32, 0, lane, A + base, B + base, C + base, D + base, XH + base, XL + base,
-                               nullptr, nullptr, nullptr, red);
+                               nullptr, nullptr, nullptr, red, &rbar[warp], warp, rpar);
           }
         }
       } else if (kind == kGroup) {
@@ -811,7 +742,7 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
                             p.x + sy.off);
         } else {
           group_refine<MODE>(p, sy, kTeamThreads, tbar, ttid, A + base, B + base, C + base, D + base, XH + base,
-                             XL + base, tR, tX, tF, red);
+                             XL + base, tR, tX, tF, red, &rbar[kRagWarps + team], kRagWarps + team, rpar);
         }
       } else {
         record_error(p.status, TRIDI_DEVERR_BAD_PLAN);  // a CTA-wide item after the team phase began

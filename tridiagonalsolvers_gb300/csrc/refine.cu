@@ -9,11 +9,15 @@
 //     r = d - T x_{k+1}                   (FP64; stored as FP32 for the next solve)
 //     rel_s = ||r_s|| / ||d_s|| per system; stop when max_s rel_s <= tol
 //     e_{k+1} = solve32(T, r)             (the same FP32 kernels as a plain solve)
-// The update and the residual are one kernel (refine_update_residual); x is
-// ping-ponged between two FP64 buffers so neighbours are read before they
-// are rewritten.  Only those two steps touch FP64 arithmetic.
+// The update and the residual are one kernel; x is ping-ponged between two
+// 8-byte-per-row buffers so neighbours are read before they are rewritten.
+// Only those two steps run in extended precision: native FP64, or (the
+// default, TRIDI_TUNE_RESIDUAL) double-float, x held as (hi, lo) FP32 pairs
+// in the same buffers and assembled into FP64 once at the end.
+#include <algorithm>
 #include <cmath>
 
+#include "dfloat.cuh"
 #include "runtime.h"
 #include "tridi_device.cuh"
 
@@ -31,7 +35,7 @@ struct RefineParams {
   const float *a, *b, *c, *d;
   const float* e;     // FP32 correction
   const double* xin;  // x_k (ignored when first)
-  double* xout;       // x_{k+1}
+  double* xout;       // x_{k+1} (double-float mode: (hi, lo) FP32 pairs in the same 8 bytes)
   float* r;           // FP32 copy of the residual
   double* rr;         // per-system sum of r^2 (accumulated)
   double* dd;         // per-system sum of d^2 (accumulated on the first sweep)
@@ -41,38 +45,79 @@ struct RefineParams {
   int rows_per_block;  // contiguous: elements per block per system chunk; interleaved: rows per block
 };
 
-// x_{k+1} at (i, s) without writing it: x_k + e (or e on the first sweep).
-__device__ __forceinline__ double xnew(const RefineParams& p, long k) {
-  return p.first ? (double)p.e[k] : p.xin[k] + (double)p.e[k];
-}
+// x_{k+1} at (i, s) without writing it: x_k + e (or e on the first sweep),
+// as a double (FP64 mode) or a double-float pair (double-float mode).
+template <bool DF>
+struct XNext;
+template <>
+struct XNext<false> {
+  using V = double;
+  __device__ __forceinline__ static V get(const RefineParams& p, long k) {
+    return p.first ? (double)p.e[k] : p.xin[k] + (double)p.e[k];
+  }
+  __device__ __forceinline__ static void put(const RefineParams& p, long k, V v) { p.xout[k] = v; }
+  __device__ __forceinline__ static V zero() { return 0.0; }
+  // d - T x at row i, and d^2; r in FP64, returned rounded to FP32
+  __device__ __forceinline__ static float residual(const RefineParams& p, long i, long k, long stride, V xi,
+                                                   float* dsq) {
+    const double di = (double)p.d[k];
+    double r = di - (double)p.b[k] * xi;
+    if (i > 0) r -= (double)p.a[k] * get(p, k - stride);
+    if (i < p.n - 1) r -= (double)p.c[k] * get(p, k + stride);
+    *dsq = p.d[k] * p.d[k];
+    return (float)r;
+  }
+};
+template <>
+struct XNext<true> {
+  using V = float2;
+  __device__ __forceinline__ static V get(const RefineParams& p, long k) {
+    return p.first ? make_float2(p.e[k], 0.f) : df_add(reinterpret_cast<const float2*>(p.xin)[k], p.e[k]);
+  }
+  __device__ __forceinline__ static void put(const RefineParams& p, long k, V v) {
+    reinterpret_cast<float2*>(p.xout)[k] = v;
+  }
+  __device__ __forceinline__ static V zero() { return make_float2(0.f, 0.f); }
+  __device__ __forceinline__ static float residual(const RefineParams& p, long i, long k, long stride, V xi,
+                                                   float* dsq) {
+    const V xm = i > 0 ? get(p, k - stride) : zero();
+    const V xp = i < p.n - 1 ? get(p, k + stride) : zero();
+    *dsq = p.d[k] * p.d[k];
+    return df_residual(i > 0 ? p.a[k] : 0.f, p.b[k], i < p.n - 1 ? p.c[k] : 0.f, p.d[k], xm, xi, xp);
+  }
+};
 
-__device__ __forceinline__ double residual_at(const RefineParams& p, long i, long k, long stride, double xi,
-                                              double* dsq) {
-  const double di = (double)p.d[k];
-  double r = di - (double)p.b[k] * xi;
-  if (i > 0) r -= (double)p.a[k] * xnew(p, k - stride);
-  if (i < p.n - 1) r -= (double)p.c[k] * xnew(p, k + stride);
-  *dsq = di * di;
-  return r;
+// The final double-float x assembled into FP64 (in place when src == dst:
+// each element is read before it is written, by the same thread).
+__global__ void __launch_bounds__(256) refine_df_to_fp64_kernel(const float2* src, double* dst, long count) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
+    const float2 v = src[k];
+    dst[k] = df_to_double(v.x, v.y);
+  }
 }
 
 // Contiguous layout: block (system s, chunk q) covers rows [q*R, q*R + R).
+// Per-thread norm partial sums in FP32 (a few rows each), the block's sums
+// in FP64.
+template <bool DF>
 __global__ void __launch_bounds__(256) refine_contig_kernel(RefineParams p) {
+  using X = XNext<DF>;
   const long chunks = (p.n + p.rows_per_block - 1) / p.rows_per_block;
   const long s = blockIdx.x / chunks, q = blockIdx.x % chunks;
-  double rs = 0.0, ds = 0.0;
+  float rsf = 0.f, dsf = 0.f;
   const long i0 = q * p.rows_per_block;
   const long i1 = i0 + p.rows_per_block < p.n ? i0 + p.rows_per_block : p.n;
   for (long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
     const long k = s * p.n + i;
-    const double xi = xnew(p, k);
-    double dsq;
-    const double r = residual_at(p, i, k, 1, xi, &dsq);
-    p.xout[k] = xi;
-    p.r[k] = (float)r;
-    rs += r * r;
-    ds += dsq;
+    const typename X::V xi = X::get(p, k);
+    float dsq;
+    const float r = X::residual(p, i, k, 1, xi, &dsq);
+    X::put(p, k, xi);
+    p.r[k] = r;
+    rsf = fmaf(r, r, rsf);
+    dsf += dsq;
   }
+  double rs = rsf, ds = dsf;
   __shared__ double red[2][8];
   for (int o = 16; o > 0; o >>= 1) {
     rs += __shfl_down_sync(kFull, rs, o);
@@ -95,26 +140,29 @@ __global__ void __launch_bounds__(256) refine_contig_kernel(RefineParams p) {
 }
 
 // Interleaved layout: block = 32 systems x 8 row lanes, rows [q*R, q*R + R).
+template <bool DF>
 __global__ void __launch_bounds__(256) refine_inter_kernel(RefineParams p) {
+  using X = XNext<DF>;
   const long groups = (p.m + 31) / 32;
   const long g = blockIdx.x % groups, q = blockIdx.x / groups;
   const long s = g * 32 + (threadIdx.x & 31);
   const int lr = threadIdx.x >> 5;
-  double rs = 0.0, ds = 0.0;
+  float rsf = 0.f, dsf = 0.f;
   const long i0 = q * p.rows_per_block;
   const long i1 = i0 + p.rows_per_block < p.n ? i0 + p.rows_per_block : p.n;
   if (s < p.m) {
     for (long i = i0 + lr; i < i1; i += 8) {
       const long k = i * p.m + s;
-      const double xi = xnew(p, k);
-      double dsq;
-      const double r = residual_at(p, i, k, p.m, xi, &dsq);
-      p.xout[k] = xi;
-      p.r[k] = (float)r;
-      rs += r * r;
-      ds += dsq;
+      const typename X::V xi = X::get(p, k);
+      float dsq;
+      const float r = X::residual(p, i, k, p.m, xi, &dsq);
+      X::put(p, k, xi);
+      p.r[k] = r;
+      rsf = fmaf(r, r, rsf);
+      dsf += dsq;
     }
   }
+  const double rs = rsf, ds = dsf;
   __shared__ double red[2][8][32];
   red[0][lr][threadIdx.x & 31] = rs;
   red[1][lr][threadIdx.x & 31] = ds;
@@ -228,6 +276,9 @@ tridi_status refine_device(const float* a, const float* b, const float* c, const
   const RefineWs w = carve(ws, n, m, layout);
   cudaStream_t st = as_stream(stream);
   cudaError_t e;
+  const int res = tunable(TRIDI_TUNE_RESIDUAL);
+  if (res != 0 && res != TRIDI_RESIDUAL_DF && res != TRIDI_RESIDUAL_FP64) return TRIDI_ERROR_INVALID_VALUE;
+  const bool df = res != TRIDI_RESIDUAL_FP64;
   tridi_status ts = solve32(a, b, c, d, w.e, n, m, layout, w, stream);
   if (ts != TRIDI_SUCCESS) return ts;
   if ((e = cudaMemsetAsync(w.dd, 0, sizeof(double) * m, st)) != cudaSuccess) return cuda_status(e);
@@ -250,12 +301,18 @@ tridi_status refine_device(const float* a, const float* b, const float* c, const
       p.rows_per_block = n < 2048 ? (int)n : 2048;
       const long chunks = (n + p.rows_per_block - 1) / p.rows_per_block;
       blocks = (unsigned)(m * chunks);
-      refine_contig_kernel<<<blocks, 256, 0, st>>>(p);
+      if (df)
+        refine_contig_kernel<true><<<blocks, 256, 0, st>>>(p);
+      else
+        refine_contig_kernel<false><<<blocks, 256, 0, st>>>(p);
     } else {
       p.rows_per_block = 256;
       const long groups = (m + 31) / 32, chunks = (n + 255) / 256;
       blocks = (unsigned)(groups * chunks);
-      refine_inter_kernel<<<blocks, 256, 0, st>>>(p);
+      if (df)
+        refine_inter_kernel<true><<<blocks, 256, 0, st>>>(p);
+      else
+        refine_inter_kernel<false><<<blocks, 256, 0, st>>>(p);
     }
     cur = (p.xout == x) ? 0 : 1;
     refine_maxrel_kernel<<<1, 1024, 0, st>>>(w.rr, w.dd, m, w.scalar);
@@ -267,9 +324,16 @@ tridi_status refine_device(const float* a, const float* b, const float* c, const
     ts = solve32(a, b, c, w.r, w.e, n, m, layout, w, stream);
     if (ts != TRIDI_SUCCESS) return ts;
   }
-  if (cur != 0 &&
-      (e = cudaMemcpyAsync(x, bufs[cur], sizeof(double) * n * m, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
+  if (df) {  // x_k as double-float pairs in bufs[cur] -> FP64 in x
+    const long count = n * m;
+    const unsigned blocks = (unsigned)std::min<long>((count + 255) / 256, 65535L * 8);
+    refine_df_to_fp64_kernel<<<blocks, 256, 0, st>>>(reinterpret_cast<const float2*>(bufs[cur]), x, count);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+  } else if (cur != 0 &&
+             (e = cudaMemcpyAsync(x, bufs[cur], sizeof(double) * n * m, cudaMemcpyDeviceToDevice, st)) !=
+                 cudaSuccess) {
     return cuda_status(e);
+  }
   if (sweeps_out) *sweeps_out = sweep;
   if (res_out) *res_out = rel;
   return rel <= tol ? TRIDI_SUCCESS : TRIDI_ERROR_NOT_CONVERGED;

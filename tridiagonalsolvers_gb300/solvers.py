@@ -120,10 +120,13 @@ def solve_large(a, b, c, d, system_size, num_systems, layout="contiguous", x=Non
     return x
 
 
-def refine(a, b, c, d, system_size, num_systems, layout="contiguous", tol=1e-10, max_sweeps=10, x=None):
-    """FP32 solves + FP64 residual refinement (tridi_refine_f32).  a..d float32
-    CUDA tensors (flat, n*m), returns (x float64, sweeps, max relative residual).
-    Raises TridiError if the tolerance is not met within max_sweeps."""
+def refine(a, b, c, d, system_size, num_systems, layout="contiguous", tol=1e-10, max_sweeps=10, x=None,
+           residual="df"):
+    """FP32 solves + extended-precision residual refinement (tridi_refine_f32):
+    residual and update in double-float ("df", FP32 pairs) or native FP64
+    ("fp64").  a..d float32 CUDA tensors (flat, n*m), returns (x float64,
+    sweeps, max relative residual).  Raises TridiError if the tolerance is not
+    met within max_sweeps."""
     torch = _torch()
     lay = {"contiguous": 0, "interleaved": 1}[layout]
     n, m = int(system_size), int(num_systems)
@@ -138,9 +141,15 @@ def refine(a, b, c, d, system_size, num_systems, layout="contiguous", tol=1e-10,
     sweeps = ctypes.c_int(0)
     rel = ctypes.c_double(0.0)
     stream = ctypes.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
-    check(L.tridi_refine_f32(a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), x.data_ptr(), n, m, lay,
-                             float(tol), int(max_sweeps), ws.data_ptr(), wsb, stream, ctypes.byref(sweeps),
-                             ctypes.byref(rel)), f"tridi_refine_f32(n={n}, m={m}, {layout})")
+    mode = {"df": 1, "fp64": 2}[residual]  # TRIDI_RESIDUAL_DF / TRIDI_RESIDUAL_FP64
+    prev = L.tridi_get_tunable(4)  # TRIDI_TUNE_RESIDUAL
+    check(L.tridi_set_tunable(4, mode), "tridi_set_tunable")
+    try:
+        check(L.tridi_refine_f32(a.data_ptr(), b.data_ptr(), c.data_ptr(), d.data_ptr(), x.data_ptr(), n, m, lay,
+                                 float(tol), int(max_sweeps), ws.data_ptr(), wsb, stream, ctypes.byref(sweeps),
+                                 ctypes.byref(rel)), f"tridi_refine_f32(n={n}, m={m}, {layout})")
+    finally:
+        L.tridi_set_tunable(4, prev)
     return x, sweeps.value, rel.value
 
 
