@@ -63,3 +63,31 @@ def test_large_full_size_1024x65536_interleaved(cuda):
     cols = np.array([0, 1, 31, 32, 511, 1000, 1023])
     xs = x.view(n, m)[:, cols].cpu().numpy()
     check_against_oracle(a[:, cols], b[:, cols], c[:, cols], d[:, cols], xs, layout=1, **WEAK)
+
+
+@pytest.mark.parametrize("n,m", [(5000, 64), (65536, 32), (300, 96), (20000, 48)])
+def test_large_interleaved_tma_passes_match_register_passes(cuda, n, m):
+    """Interleaved FP32 with m a multiple of 32 runs the TMA-tiled reduce and
+    back passes; they agree with the register-kernel passes (forced with
+    TRIDI_TUNE_LARGE_TMA = 2) and with the FP64 oracle.  m = 48 takes the
+    register passes either way."""
+    import torch
+
+    from tridiagonalsolvers_gb300 import _lib
+
+    L = _lib.lib()
+    a, b, c, d = workloads.weak(m, n, seed=n + m, layout=1)
+    t = [torch.from_numpy(np.ascontiguousarray(v).ravel()).to(cuda) for v in (a, b, c, d)]
+    outs = []
+    for mode in (0, 2):
+        L.tridi_set_tunable(6, mode)
+        try:
+            outs.append(tg.solve_large(*t, n, m, layout="interleaved").cpu().numpy())
+        finally:
+            L.tridi_set_tunable(6, 0)
+    x_tma, x_reg = outs
+    scale = np.abs(x_reg).max()
+    assert np.abs(x_tma - x_reg).max() <= 1e-5 * scale
+    xs = x_tma.reshape(n, m)
+    res = gold.rel_residual(a, b, c, d, xs, layout=1)
+    assert res.max() <= 1e-5, f"residual {res.max():.2e}"

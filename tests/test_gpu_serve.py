@@ -79,3 +79,24 @@ def test_admission_by_footprint_and_overlap(cuda):
         del big
     finally:
         srv.close()
+
+
+def test_large_and_small_requests_in_one_batch(cuda):
+    """Requests of 2^18 rows or more take the direct copies, smaller ones the
+    pinned staging, in the same batch: every answer reaches the target."""
+    from tridiagonalsolvers_gb300 import workloads
+
+    rng = np.random.default_rng(21)
+    a, b, c, d, off = workloads.adi(np.full(100, 4000), seed=3)
+    big = (a, b, c, d, off)  # 400000 rows
+    smalls = [make_request(rng, max_systems=30) for _ in range(5)]
+    srv = Server(hbm_budget_bytes=4 << 30, max_inflight=1)
+    try:
+        reqs = [smalls[0], big] + smalls[1:]
+        ids = [srv.submit(*r) for r in reqs]
+        for r, i in zip(reqs, ids):
+            x, info = srv.wait(i)
+            assert info["rel_residual"] <= 1e-10
+            _check(r, x)
+    finally:
+        srv.close()

@@ -15,6 +15,8 @@
 //      per-system Thomas kernel for interleaved batches of <= 256 rows.
 //   3. large_back: each chunk is read and eliminated again and its rows
 //      recovered from the two separators around it.
+// For the interleaved FP32 layout with m a multiple of 32, steps 1 and 3 run
+// as TMA-tiled persistent kernels (large_tma.cu) on the same chunks.
 // Memory traffic per unknown: inputs read twice (2 x 16 B FP32), x written
 // once (4 B), plus ~20/L B of interface data.  No reference kernel
 // corresponds; the reference's large-system path is pcrGauss's global-memory
@@ -27,6 +29,9 @@ namespace tridi {
 template <class T>
 tridi_status partition_solve_device(const T* a, const T* b, const T* c, const T* d, T* x, int n, int m,
                                     tridi_stream_t stream);
+bool large_tma_ok(const float* a, const float* b, const float* c, const float* d, long n, long m);
+tridi_status large_tma_pass(bool back, const float* a, const float* b, const float* c, const float* d, long n,
+                            long m, long P, long PMp, float* iface, const float* sol, float* x, cudaStream_t st);
 
 struct LargeParams {
   const void* a;
@@ -202,7 +207,17 @@ tridi_status large_solve_device(const T* a, const T* b, const T* c, const T* d, 
   void* inner = w + (size_t)14 * p.PMp * sizeof(T) + 256;
   const size_t inner_bytes = ws_bytes - ((size_t)14 * p.PMp * sizeof(T) + 256);
   const unsigned blocks = (unsigned)((PM + 255) / 256);
-  large_reduce_kernel<T, kChunk><<<blocks, 256, 0, st>>>(p);
+  // interleaved FP32 with m a multiple of 32: the TMA-tiled passes (large_tma.cu)
+  bool tma = false;
+  if constexpr (sizeof(T) == 4) tma = layout == 1 && tunable(TRIDI_TUNE_LARGE_TMA) != 2 && large_tma_ok(a, b, c, d, n, m);
+  if (tma) {
+    const tridi_status t = large_tma_pass(false, reinterpret_cast<const float*>(a), reinterpret_cast<const float*>(b),
+                                          reinterpret_cast<const float*>(c), reinterpret_cast<const float*>(d), n, m,
+                                          p.P, p.PMp, static_cast<float*>(p.iface), nullptr, nullptr, st);
+    if (t != TRIDI_SUCCESS) return t;
+  } else {
+    large_reduce_kernel<T, kChunk><<<blocks, 256, 0, st>>>(p);
+  }
   large_assemble_kernel<T><<<blocks, 256, 0, st>>>(p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e);
@@ -215,6 +230,10 @@ tridi_status large_solve_device(const T* a, const T* b, const T* c, const T* d, 
     ts = large_solve_device<T>(r, r + p.PMp, r + 2 * p.PMp, r + 3 * p.PMp, static_cast<T*>(p.sol), p.P, m, layout,
                                inner, inner_bytes, stream);
   if (ts != TRIDI_SUCCESS) return ts;
+  if (tma)
+    return large_tma_pass(true, reinterpret_cast<const float*>(a), reinterpret_cast<const float*>(b),
+                          reinterpret_cast<const float*>(c), reinterpret_cast<const float*>(d), n, m, p.P, p.PMp,
+                          nullptr, static_cast<const float*>(p.sol), reinterpret_cast<float*>(x), st);
   large_back_kernel<T, kChunk><<<blocks, 256, 0, st>>>(p);
   return cuda_status(cudaGetLastError());
 }

@@ -1,0 +1,256 @@
+// TMA-tiled passes of the large-system solver for the interleaved FP32
+// layout (element i of system s at i*m + s, m a multiple of 32).
+//
+// The two passes of large.cu that read the coefficients -- large_reduce
+// (chunk elimination, interface out) and large_back (elimination again, back
+// substitution, x out) -- as persistent kernels: one CTA per SM, a producer
+// warp that streams tiles of kTileRows rows x 32 systems of a, b, c, d into a
+// kStages-deep shared-memory ring with cp.async.bulk.tensor.2d (one tensor
+// map per array), and 8 consumer warps.  Warp w of a tile owns rows
+// [w*16, w*16 + 16) of it, lane l system s0 + l: exactly the chunks (16 rows
+// of one system) of the register kernels, so the interface arrays, the
+// separator assembly and the recursion are shared with them.  A lane reads
+// its column of the tile (row stride 32 words: lane l always on bank l, no
+// conflicts), eliminates it in place, and writes its interface (reduce) or
+// its 16 unknowns (back) straight to global memory: consecutive lanes,
+// consecutive systems, one 128-byte line per row.
+//
+// Against the register kernels (one thread per chunk, 64 prefetched values
+// and the chunk's eliminated rows in registers, two blocks per SM) the ring
+// keeps 128 KB of loads in flight per SM whatever the compute is doing.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+
+#include "partition.cuh"
+#include "runtime.h"
+
+namespace tridi {
+
+namespace {
+constexpr int kLtWarps = 8;                  // consumer warps
+constexpr int kLtChunk = 16;                 // rows per lane (= the register kernels' chunk)
+constexpr int kTileRows = kLtWarps * kLtChunk;  // 128
+constexpr int kTileCols = 32;                // systems per tile
+constexpr int kStages = 3;
+constexpr int kTileFloats = kTileRows * kTileCols;  // per array
+constexpr size_t kLtSmem = 128 + (size_t)kStages * 4 * kTileFloats * sizeof(float);  // 192 KB + barriers
+
+struct LtParams {
+  long n, m, P, PMp;
+  float* iface;     // reduce: 10 arrays of P*m (stride PMp)
+  const float* sol; // back: separators
+  float* x;         // back: solution
+  int row_tiles, col_tiles;
+  unsigned* status;
+};
+
+__device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Chunk elimination of one lane's column (rows 0..k-1 at stride 32 words),
+// in place, and its interface (partition.cuh's Chunk summary).
+__device__ __forceinline__ void column_eliminate(ChunkSummary<float>& cs, int k, bool first, bool last,
+                                                 float* __restrict__ sa, const float* __restrict__ sb,
+                                                 float* __restrict__ sc, float* __restrict__ sd) {
+  float cprev = 0.f, aprev = 0.f, dprev = 0.f;
+#pragma unroll
+  for (int i = 0; i < kLtChunk - 1; ++i) {
+    if (i < k - 1) {
+      const int o = i * kTileCols;
+      const float a = (i == 0 && first) ? 0.f : sa[o];
+      const float inv = tdiv(1.f, sb[o] - a * cprev);
+      const float cn = sc[o] * inv;
+      const float an = (i == 0 ? a : -a * aprev) * inv;
+      const float dn = (sd[o] - a * dprev) * inv;
+      sa[o] = an; sc[o] = cn; sd[o] = dn;
+      cprev = cn; aprev = an; dprev = dn;
+    }
+  }
+  float D = 0.f, C = -1.f, A = 0.f;
+#pragma unroll
+  for (int i = kLtChunk - 2; i >= 0; --i) {
+    if (i <= k - 2) {
+      const int o = i * kTileCols;
+      const float c = sc[o];
+      D = sd[o] - c * D;
+      C = -c * C;
+      A = sa[o] - c * A;
+    }
+  }
+  cs.fD = D; cs.fC = C; cs.fA = A;
+  if (k >= 2) {
+    cs.lD = dprev; cs.lC = cprev; cs.lA = aprev;
+  } else {
+    cs.lD = 0.f; cs.lC = 0.f; cs.lA = -1.f;
+  }
+  if (k >= 1) {
+    const int o = (k - 1) * kTileCols;
+    cs.sep = Row<float>{sa[o], sb[o], sc[o], sd[o]};
+    if (k == 1 && first) cs.sep.a = 0.f;
+    if (last) cs.sep.c = 0.f;
+  } else {
+    cs.sep = Row<float>{0.f, 1.f, 0.f, 0.f};
+  }
+}
+
+template <bool BACK>
+__global__ void __launch_bounds__(32 * (kLtWarps + 1), 1)
+    large_tile_kernel(LtParams p, const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb,
+                      const __grid_constant__ CUtensorMap mc, const __grid_constant__ CUtensorMap md) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* empty = full + kStages;
+  float* ring = reinterpret_cast<float*>(smem + 128);  // stage s, array q at ring + (s*4 + q) * kTileFloats
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ntiles = p.row_tiles * p.col_tiles;
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kLtWarps);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  if (warp == kLtWarps) {  // ---------------- producer ----------------
+    if (lane != 0) return;
+    int k = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
+      const int s = k % kStages;
+      if (k >= kStages && !mbar_wait(&empty[s], ((k / kStages) - 1) & 1, p.status)) return;
+      const int x0 = (t % p.col_tiles) * kTileCols, y0 = (t / p.col_tiles) * kTileRows;
+      mbar_arrive_expect_tx(&full[s], 4u * kTileFloats * sizeof(float));
+      float* st = ring + (size_t)s * 4 * kTileFloats;
+      tma_load_2d(st + 0 * kTileFloats, &ma, x0, y0, &full[s]);
+      tma_load_2d(st + 1 * kTileFloats, &mb, x0, y0, &full[s]);
+      tma_load_2d(st + 2 * kTileFloats, &mc, x0, y0, &full[s]);
+      tma_load_2d(st + 3 * kTileFloats, &md, x0, y0, &full[s]);
+    }
+    return;
+  }
+
+  // ---------------- consumers ----------------
+  int k = 0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
+    const int s = k % kStages;
+    if (!mbar_wait(&full[s], (k / kStages) & 1, p.status)) return;
+    const long sys = (long)(t % p.col_tiles) * kTileCols + lane;
+    const long r0 = (long)(t / p.col_tiles) * kTileRows + (long)warp * kLtChunk;  // the lane's first row
+    const long j = r0 / kLtChunk;                                                 // its chunk
+    float* st = ring + (size_t)s * 4 * kTileFloats + warp * kLtChunk * kTileCols + lane;
+    float* sa = st;
+    float* sb = st + kTileFloats;
+    float* sc = st + 2 * kTileFloats;
+    float* sd = st + 3 * kTileFloats;
+    const long rem = p.n - r0;
+    const int kr = rem <= 0 ? 0 : (rem < kLtChunk ? (int)rem : kLtChunk);
+    if (kr > 0) {
+      ChunkSummary<float> cs;
+      column_eliminate(cs, kr, j == 0, j == p.P - 1, sa, sb, sc, sd);
+      const long o = j * p.m + sys;
+      if constexpr (!BACK) {
+        float* f = p.iface;
+        const long S = p.PMp;
+        f[0 * S + o] = cs.fD; f[1 * S + o] = cs.fC; f[2 * S + o] = cs.fA;
+        f[3 * S + o] = cs.lD; f[4 * S + o] = cs.lC; f[5 * S + o] = cs.lA;
+        f[6 * S + o] = cs.sep.a; f[7 * S + o] = cs.sep.b; f[8 * S + o] = cs.sep.c; f[9 * S + o] = cs.sep.d;
+      } else {
+        const float sj = p.sol[o];
+        const float sl = j > 0 ? p.sol[o - p.m] : 0.f;
+        float* gx = p.x + r0 * p.m + sys;
+        gx[(long)(kr - 1) * p.m] = sj;
+        float xn = sj;
+#pragma unroll
+        for (int i = kLtChunk - 2; i >= 0; --i) {
+          if (i <= kr - 2) {
+            const int oo = i * kTileCols;
+            xn = sd[oo] - sc[oo] * xn - sa[oo] * sl;
+            gx[(long)i * p.m] = xn;
+          }
+        }
+      }
+    }
+    release_stage(&empty[s]);
+  }
+}
+
+// The driver's tensor-map encoder, looked up through the runtime once (the
+// library does not link the driver library itself, so it loads on machines
+// without one).
+PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+bool make_map(CUtensorMap* map, const float* base, long n, long m) {
+  const auto enc = encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)m, (cuuint64_t)n};
+  const cuuint64_t strides[1] = {(cuuint64_t)m * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)kTileCols, (cuuint32_t)kTileRows};
+  const cuuint32_t elem[2] = {1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, elem,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+// Whether the TMA passes apply: interleaved FP32, m a multiple of 32, 16-byte
+// aligned arrays, a chunk count that matches (P = ceil(n / 16)).
+bool large_tma_ok(const float* a, const float* b, const float* c, const float* d, long n, long m) {
+  return m % kTileCols == 0 && n >= 2 && aligned16(a) && aligned16(b) && aligned16(c) && aligned16(d) &&
+         n < (1L << 31) && m < (1L << 31);
+}
+
+// One TMA pass: back = false -> interface (reduce), true -> x (back).
+tridi_status large_tma_pass(bool back, const float* a, const float* b, const float* c, const float* d, long n,
+                            long m, long P, long PMp, float* iface, const float* sol, float* x, cudaStream_t st) {
+  const DeviceInfo* dev = current_device();
+  if (!dev) return TRIDI_ERROR_CUDA;
+  if ((size_t)dev->max_smem_optin < kLtSmem) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  CUtensorMap ma, mb, mc, md;
+  if (!make_map(&ma, a, n, m) || !make_map(&mb, b, n, m) || !make_map(&mc, c, n, m) || !make_map(&md, d, n, m))
+    return TRIDI_ERROR_INVALID_VALUE;
+  LtParams p{};
+  p.n = n; p.m = m; p.P = P; p.PMp = PMp; p.iface = iface; p.sol = sol; p.x = x;
+  p.row_tiles = (int)((n + kTileRows - 1) / kTileRows);
+  p.col_tiles = (int)(m / kTileCols);
+  p.status = dev->status;
+  const long ntiles = (long)p.row_tiles * p.col_tiles;
+  int grid = dev->sm_count;
+  if (grid > ntiles) grid = (int)ntiles;
+  cudaError_t e;
+  if (back) {
+    if ((e = cudaFuncSetAttribute(large_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kLtSmem)) != cudaSuccess)
+      return cuda_status(e);
+    large_tile_kernel<true><<<grid, 32 * (kLtWarps + 1), kLtSmem, st>>>(p, ma, mb, mc, md);
+  } else {
+    if ((e = cudaFuncSetAttribute(large_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kLtSmem)) != cudaSuccess)
+      return cuda_status(e);
+    large_tile_kernel<false><<<grid, 32 * (kLtWarps + 1), kLtSmem, st>>>(p, ma, mb, mc, md);
+  }
+  return cuda_status(cudaGetLastError());
+}
+
+}  // namespace tridi

@@ -17,10 +17,12 @@
 // Slots work concurrently, so a request that arrives while others are on the
 // GPU is admitted as soon as a slot and memory free up and its work overlaps
 // theirs on the device.  Each system's arithmetic is independent of what else
-// is in its batch.  Host transfers (TRIDI_TUNE_SERVER_COPY): by default in
-// chunks of 2^20 rows through two pinned buffers per slot, which a pool of
-// host threads fills from (and empties into) the callers' pageable arrays in
-// parallel while the copy engines move the other buffer; or plain
+// is in its batch.  Host transfers (TRIDI_TUNE_SERVER_COPY): by default,
+// requests of 2^18 rows or more move by cudaMemcpyAsync straight from and to
+// the callers' arrays, and the smaller ones, packed after them, in chunks of
+// 2^20 rows through two pinned buffers per slot, which a pool of host threads
+// fills from (and empties into) the callers' pageable arrays in parallel
+// while the copy engines move the other buffer; or plain
 // cudaMemcpyAsync on the callers' arrays; or, where the device can access
 // pageable host memory (a Grace host), kernels that read the callers' arrays
 // and write their x directly.
@@ -167,6 +169,10 @@ class CopyPool {
 };
 
 constexpr long kStageRows = 1L << 20;  // rows per pinned staging chunk (16 MB in, 8 MB out)
+// Requests of at least this many rows move by cudaMemcpyAsync straight from
+// and to the callers' arrays (the driver's pageable path runs at 100-170 GB/s
+// from 1 MB per copy up); smaller ones go through the pinned staging.
+constexpr long kDirectRows = 1L << 18;
 
 struct Request {
   long long id = 0;
@@ -388,6 +394,14 @@ class Server {
       delete b;
       return false;
     }
+    if (staged_) {  // large requests first, the staged ones in one contiguous row range after them
+      std::stable_partition(b->reqs.begin(), b->reqs.end(), [](const Request* r) { return r->rows >= kDirectRows; });
+      long row = 0;
+      for (size_t q = 0; q < b->reqs.size(); ++q) {
+        b->req_row0[q] = row;
+        row += b->reqs[q]->rows;
+      }
+    }
     b->bytes = footprint(b->rows, b->systems);
     used_ += b->bytes;
     ++batches_;
@@ -482,10 +496,22 @@ class Server {
         gather_kernel<<<cgrid, 256, 0, st>>>(djobs, da, db, dc, dd);
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
       } else if (staged_) {
-        // chunks of kStageRows rows through two pinned buffers: the pool fills
-        // one while the copy engine drains the other
+        // large requests straight from the callers' arrays; the rest in chunks
+        // of kStageRows rows through two pinned buffers: the pool fills one
+        // while the copy engine drains the other
+        long s0 = 0;  // first staged row
+        for (size_t q = 0; q < b->reqs.size() && b->reqs[q]->rows >= kDirectRows; ++q) {
+          Request* r = b->reqs[q];
+          const size_t off = (size_t)b->req_row0[q], bytes = (size_t)r->rows * 4;
+          if ((e = cudaMemcpyAsync(da + off, r->a, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+              (e = cudaMemcpyAsync(db + off, r->b, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+              (e = cudaMemcpyAsync(dc + off, r->c, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+              (e = cudaMemcpyAsync(dd + off, r->d, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return cuda_status(e);
+          s0 = b->req_row0[q] + r->rows;
+        }
         std::vector<CopyPool::Seg> segs;
-        for (long r0 = 0, k = 0; r0 < b->rows; r0 += kStageRows, ++k) {
+        for (long r0 = s0, k = 0; r0 < b->rows; r0 += kStageRows, ++k) {
           const long r1 = std::min(b->rows, r0 + kStageRows);
           float* buf = s->in_stage[k & 1];
           if (k >= 2 && (e = cudaEventSynchronize(s->in_done[k & 1])) != cudaSuccess) return cuda_status(e);
@@ -538,11 +564,21 @@ class Server {
         scatter_kernel<<<cgrid, 256, 0, st>>>(djobs, dx);
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
       } else if (staged_) {
-        // chunk k's copy engine transfer overlaps the pool's copy-out of chunk k-1
+        // large requests straight into the callers' arrays; for the staged
+        // range, chunk k's copy engine transfer overlaps the pool's copy-out
+        // of chunk k-1
+        long s0 = 0;
+        for (size_t q = 0; q < b->reqs.size() && b->reqs[q]->rows >= kDirectRows; ++q) {
+          Request* r = b->reqs[q];
+          if ((e = cudaMemcpyAsync(r->x, dx + b->req_row0[q], sizeof(double) * r->rows, cudaMemcpyDeviceToHost,
+                                   st)) != cudaSuccess)
+            return cuda_status(e);
+          s0 = b->req_row0[q] + r->rows;
+        }
         std::vector<CopyPool::Seg> segs;
-        const long nchunks = (b->rows + kStageRows - 1) / kStageRows;
+        const long nchunks = (b->rows - s0 + kStageRows - 1) / kStageRows;
         auto copy_out = [&](long k) {
-          const long r0 = k * kStageRows, r1 = std::min(b->rows, r0 + kStageRows);
+          const long r0 = s0 + k * kStageRows, r1 = std::min(b->rows, r0 + kStageRows);
           const double* buf = s->out_stage[k & 1];
           segs.clear();
           for (size_t q = 0; q < b->reqs.size(); ++q) {
@@ -553,7 +589,7 @@ class Server {
           pool_->run(segs);
         };
         for (long k = 0; k < nchunks; ++k) {
-          const long r0 = k * kStageRows, r1 = std::min(b->rows, r0 + kStageRows);
+          const long r0 = s0 + k * kStageRows, r1 = std::min(b->rows, r0 + kStageRows);
           if ((e = cudaMemcpyAsync(s->out_stage[k & 1], dx + r0, sizeof(double) * (r1 - r0), cudaMemcpyDeviceToHost,
                                    st)) != cudaSuccess ||
               (e = cudaEventRecord(s->out_done[k & 1], st)) != cudaSuccess)
@@ -563,8 +599,10 @@ class Server {
             copy_out(k - 1);
           }
         }
-        if ((e = cudaEventSynchronize(s->out_done[(nchunks - 1) & 1])) != cudaSuccess) return cuda_status(e);
-        copy_out(nchunks - 1);
+        if (nchunks > 0) {
+          if ((e = cudaEventSynchronize(s->out_done[(nchunks - 1) & 1])) != cudaSuccess) return cuda_status(e);
+          copy_out(nchunks - 1);
+        }
       } else {
         for (size_t q = 0; q < b->reqs.size(); ++q) {
           Request* r = b->reqs[q];
