@@ -12,7 +12,7 @@
 //      P = ceil(n/L) separators per system form a batch of the same kind,
 //      solved by the uniform partition solver (contiguous, P <= 8704) or by
 //      this scheme again (interleaved, or larger P), down to a one-thread-
-//      per-system Thomas kernel for interleaved batches of <= 256 rows.
+//      per-system Thomas kernel for interleaved batches of <= 32 rows.
 //   3. large_back: each chunk is read and eliminated again and its rows
 //      recovered from the two separators around it.
 // For the interleaved FP32 layout with m a multiple of 32, steps 1 and 3 run
@@ -138,8 +138,10 @@ __global__ void __launch_bounds__(256) large_back_kernel(LargeParams p) {
 // keeping c' and d' in a scratch array; a warp reads 32 consecutive systems,
 // so every row access is coalesced.
 template <class T>
-__global__ void __launch_bounds__(256) thomas_interleaved_kernel(const T* a, const T* b, const T* c, const T* d,
-                                                                 T* x, long n, long m, T* cp, T* dp) {
+__global__ void __launch_bounds__(256) thomas_interleaved_kernel(const T* __restrict__ a, const T* __restrict__ b,
+                                                                 const T* __restrict__ c, const T* __restrict__ d,
+                                                                 T* __restrict__ x, long n, long m,
+                                                                 T* __restrict__ cp, T* __restrict__ dp) {
   const long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= m) return;
   T cprev = T(0), dprev = T(0);
@@ -164,7 +166,10 @@ __global__ void __launch_bounds__(256) thomas_interleaved_kernel(const T* a, con
 
 namespace {
 constexpr int kChunk = 16;
-constexpr long kThomasMax = 256;  // interleaved base case
+// Interleaved base case: one thread per system, a serial chain over n rows
+// with only m threads in flight, so it is kept short (the recursion goes one
+// level further rather than run 256-row chains on 1024 threads).
+constexpr long kThomasMax = 32;
 
 long round64(long v) { return (v + 63) & ~63L; }
 

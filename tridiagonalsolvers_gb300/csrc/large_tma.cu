@@ -154,9 +154,14 @@ __global__ void __launch_bounds__(32 * (kLtWarps + 1), 1)
     const long rem = p.n - r0;
     const int kr = rem <= 0 ? 0 : (rem < kLtChunk ? (int)rem : kLtChunk);
     if (kr > 0) {
+      const long o = j * p.m + sys;
+      float sj = 0.f, sl = 0.f;
+      if constexpr (BACK) {  // the separators' loads overlap the elimination
+        sj = p.sol[o];
+        sl = j > 0 ? p.sol[o - p.m] : 0.f;
+      }
       ChunkSummary<float> cs;
       column_eliminate(cs, kr, j == 0, j == p.P - 1, sa, sb, sc, sd);
-      const long o = j * p.m + sys;
       if constexpr (!BACK) {
         float* f = p.iface;
         const long S = p.PMp;
@@ -164,8 +169,6 @@ __global__ void __launch_bounds__(32 * (kLtWarps + 1), 1)
         f[3 * S + o] = cs.lD; f[4 * S + o] = cs.lC; f[5 * S + o] = cs.lA;
         f[6 * S + o] = cs.sep.a; f[7 * S + o] = cs.sep.b; f[8 * S + o] = cs.sep.c; f[9 * S + o] = cs.sep.d;
       } else {
-        const float sj = p.sol[o];
-        const float sl = j > 0 ? p.sol[o - p.m] : 0.f;
         float* gx = p.x + r0 * p.m + sys;
         gx[(long)(kr - 1) * p.m] = sj;
         float xn = sj;
