@@ -217,42 +217,34 @@ struct XStore {
 
 // Adds (rr, dd) over a solve group, and its leader folds sqrt(rr) / sqrt(dd)
 // into the CTA's maximum `rel` (shared memory; the kernel folds it into the
-// batch maximum once at the end).  red: 2 doubles per warp of the CTA.
-__device__ __forceinline__ void group_rel_max(float rr, float dd, int gt, int bar, int gtid, double* red,
+// batch maximum once at the end).  The sums stay in FP32, like the per-lane
+// partials (GB300's FP64 adds, square roots and divisions are slow): enough
+// for a residual check, and valid while the squares stay in FP32's range
+// (|d| and |d - Tx| above ~1e-19 where not zero).  red: 2 floats per warp.
+__device__ __forceinline__ void group_rel_max(float rr, float dd, int gt, int bar, int gtid, float* red,
                                               unsigned long long* rel) {
-  double r2 = rr, d2 = dd;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    r2 += __shfl_down_sync(kFull, r2, o);
-    d2 += __shfl_down_sync(kFull, d2, o);
+    rr += __shfl_down_sync(kFull, rr, o);
+    dd += __shfl_down_sync(kFull, dd, o);
   }
   if (gt > 32) {
     const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-      red[2 * w] = r2;
-      red[2 * w + 1] = d2;
+      red[2 * w] = rr;
+      red[2 * w + 1] = dd;
     }
     group_sync(bar, gt);
     if (gtid == 0) {
       for (int q = 1; q < gt / 32; ++q) {
-        r2 += red[2 * (w + q)];
-        d2 += red[2 * (w + q) + 1];
+        rr += red[2 * (w + q)];
+        dd += red[2 * (w + q) + 1];
       }
     }
   }
   if (gtid == 0) {
-    // sqrt(r2 / d2) in FP32 (GB300's FP64 square root and division are slow):
-    // both sums scaled by a power of two that brings d2 near 1 first, so
-    // neither underflows in FP32
-    double v;
-    const int e = ((__double2hiint(d2) >> 20) & 0x7ff) - 1023;
-    if (d2 > 0.0 && e > -1000 && e < 1000) {
-      const double sc = __hiloint2double((1023 - e) << 20, 0);  // 2^-e
-      v = (double)(sqrtf((float)(r2 * sc)) / sqrtf((float)(d2 * sc)));
-    } else {
-      v = d2 > 0.0 ? sqrt(r2) / sqrt(d2) : sqrt(r2);
-    }
-    atomicMax(rel, (unsigned long long)__double_as_longlong(v));  // the CTA's maximum, in shared memory
+    const float v = dd > 0.f ? sqrtf(rr) / sqrtf(dd) : sqrtf(rr);
+    atomicMax(rel, (unsigned long long)__double_as_longlong((double)v));  // the CTA's maximum, in shared memory
   }
 }
 
@@ -409,7 +401,8 @@ __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& s
     dd = fmaf(d, d, dd);
     xo[i] = xs.get64(i);
   }
-  group_rel_max(rr, dd, gt, bar, gtid, red, reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps));
+  group_rel_max(rr, dd, gt, bar, gtid, reinterpret_cast<float*>(red),
+                reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps));
 }
 
 // A BIG system (rows read straight from global memory, right-hand side rhs):
@@ -518,7 +511,8 @@ __device__ __forceinline__ void big_refine(const RagParams& p, const RagSys& sy,
     dd = fmaf(d, d, dd);
     xo[i] = xs.get64(i);
   }
-  group_rel_max(rr, dd, kRagThreads, 1, tid, red, reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps));
+  group_rel_max(rr, dd, kRagThreads, 1, tid, reinterpret_cast<float*>(red),
+                reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps));
   consumer_sync(kRagThreads);
 }
 
