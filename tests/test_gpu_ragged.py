@@ -78,13 +78,14 @@ def test_ragged_full_workload_100000_systems(cuda):
 def test_ragged_refined_graph_replay(cuda, residual):
     """Fused refinement of a ragged batch (every item kind: warp, 160-thread
     group, whole CTA in the ring, and systems beyond the ring refined from
-    global memory, up to 24480 rows) to 1e-10, captured once in a CUDA graph;
+    global memory, up to 24480 rows; 13000 and 13560 rows fit the ring of the
+    one-correction form only) to 1e-10, captured once in a CUDA graph;
     replays agree bit for bit with the eager launch and with the FP64 oracle."""
     from tridiagonalsolvers_gb300.ragged import RaggedRefiner
 
     rng = np.random.default_rng(3)
     sizes = np.concatenate([rng.integers(32, 480, 200), rng.integers(480, 12280, 40), rng.integers(12281, 24481, 6),
-                            [16384, 24480]])
+                            [13000, 13560, 16384, 24480]])
     a, b, c, d, off = workloads.adi(sizes, seed=5)
     total = int(off[-1])
     t = [_dev(cuda, v, total) for v in (a, b, c, d)]
@@ -151,10 +152,11 @@ def test_ragged_rejects_oversize_systems():
 
 
 def test_double_float_to_fp64_is_correctly_rounded(cuda):
-    """The refinement's FP64 output assembly (integer fast path + FP64 add
-    fallback) equals numpy's correctly rounded float64(hi) + float64(lo) for
-    normalised pairs, including lo finer than hi's double ulp, hi a power of
-    two with lo of the opposite sign, zeros and subnormal lo."""
+    """The refinement's FP64 output assembly (scaled-conversion fast path +
+    FP64 add fallback) equals numpy's correctly rounded float64(hi) +
+    float64(lo) for normalised pairs, including lo finer than hi's double ulp,
+    exact ties at a half and a quarter of that ulp, hi a power of two with lo
+    of the opposite sign, zeros, tiny hi and subnormal lo."""
     import ctypes
 
     import torch
@@ -172,6 +174,13 @@ def test_double_float_to_fp64_is_correctly_rounded(cuda):
     lo = (frac * ulp).astype(np.float32)
     lo[::7] = 0.0
     lo[4200:4300] = np.float32(1e-42)  # subnormal
+    # ties: odd multiples of a half, quarter or eighth of hi's double ulp
+    k = 20000
+    du = np.spacing(np.abs(hi[5000:5000 + k]).astype(np.float64)) * 2.0 ** -29
+    odd = (2 * rng.integers(1, 1 << 20, k) + 1).astype(np.float64)
+    tie = odd * du * 2.0 ** -rng.integers(1, 4, k).astype(np.float64) * rng.choice([-1.0, 1.0], k)
+    tf = tie.astype(np.float32)
+    lo[5000:5000 + k] = np.where(tf.astype(np.float64) == tie, tf, np.float32(0))
     # keep pairs normalised after rounding lo to float
     bad = np.abs(lo.astype(np.float64)) > 0.5 * ulp
     lo[bad] = 0.0

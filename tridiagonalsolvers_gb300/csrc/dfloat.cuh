@@ -21,23 +21,27 @@ __device__ __forceinline__ double f2d_exact(float f) {
   return (double)f;
 }
 
-// The double nearest hi + lo for a normalised double-float pair
-// (|lo| <= ulp_float(hi) / 2), mostly without the FP64 pipe: when lo is a
-// whole number K of hi's double ulps (its lowest set bit no finer than that
-// ulp, i.e. float exponent of lo >= exponent of hi - 29), hi + lo is exactly
-// representable and its bit pattern is hi's plus or minus K (the sum stays in
-// hi's binade, except when hi is a power of two and lo pulls it below: that
-// case, lo finer than the ulp, and non-normal inputs take one FP64 add).
+// The double nearest hi + lo (ties to even) for a normalised double-float
+// pair (|lo| <= ulp_float(hi) / 2), without the FP64 pipe.  With u = hi's
+// double ulp, k = lo / u rounded half to even is one exact FP32 scaling by a
+// power of two and one float -> int conversion (|k| <= 2^28).  hi + lo stays
+// in hi's binade (it cannot reach the next power of two, and cannot fall
+// below hi's own unless hi is a power of two and lo has the opposite sign),
+// so the result's bit pattern is hi's moved by k units, and as hi's double
+// has 29 zero low bits, k's parity is the sum's: the ties go to even.  hi
+// below 2^-75 (where 1/u leaves FP32's range), non-normal hi and a
+// power-of-two hi under a negative lo take one FP64 add.
 __device__ __forceinline__ double df_to_double(float hi, float lo) {
   const unsigned uh = __float_as_uint(hi), ul = __float_as_uint(lo);
-  const int eh = (int)((uh >> 23) & 0xffu), el = (int)((ul >> 23) & 0xffu);
-  if ((ul & 0x7fffffffu) == 0u) return f2d_exact(hi);
-  const int sh = el - eh + 29;  // lo = +-Ml * 2^sh ulps of hi's double
-  const bool opposite = ((uh ^ ul) >> 31) != 0u;
-  if (eh >= 1 && eh <= 254 && el >= 1 && sh >= 0 && !(opposite && (uh & 0x7fffffu) == 0u)) {
-    const long long H = __double_as_longlong(f2d_exact(hi));
-    const long long K = (long long)((ul & 0x7fffffu) | 0x800000u) << sh;
-    return __longlong_as_double(opposite ? H - K : H + K);
+  const unsigned eh = (uh >> 23) & 0xffu;
+  const bool pow2_down = ((uh ^ ul) >> 31) != 0u && (uh & 0x7fffffu) == 0u && (ul & 0x7fffffffu) != 0u;
+  if (eh >= 52u && eh <= 254u && !pow2_down) {
+    const float inv_u = __uint_as_float((306u - eh) << 23);  // 2^(52 - unbiased exponent of hi)
+    const int k = __float2int_rn(__fmul_rn(lo, inv_u));
+    if (k >= -(1 << 28) && k <= (1 << 28)) {
+      const long long h = __double_as_longlong(f2d_exact(hi));
+      return __longlong_as_double((int)uh < 0 ? h - k : h + k);
+    }
   }
   return f2d_exact(hi) + f2d_exact(lo);
 }
@@ -66,12 +70,12 @@ __device__ __forceinline__ float2 df_add(float2 x, float v) {
   return make_float2(hi, lo);
 }
 
-// d - a xm - b x0 - c xp for double-float x, rounded to FP32: products of
-// the high words exactly (TwoProd by FMA), summed with TwoSum; the low
-// words' products and all rounding errors gathered in one FP32 term.
-__device__ __forceinline__ float df_residual(float a, float b, float c, float d, float2 xm, float2 x0, float2 xp) {
-  const float pb = __fmul_rn(b, x0.x), pa = __fmul_rn(a, xm.x), pc = __fmul_rn(c, xp.x);
-  float t = -(fmaf(b, x0.x, -pb) + fmaf(a, xm.x, -pa) + fmaf(c, xp.x, -pc));
+// d - a xm - b x0 - c xp for FP32 x, as an unevaluated sum s + t: the
+// products exactly (TwoProd by FMA), summed with TwoSum, their rounding
+// errors gathered in the FP32 term t.
+__device__ __forceinline__ float2 residual_parts(float a, float b, float c, float d, float xm, float x0, float xp) {
+  const float pb = __fmul_rn(b, x0), pa = __fmul_rn(a, xm), pc = __fmul_rn(c, xp);
+  float t = -(fmaf(b, x0, -pb) + fmaf(a, xm, -pa) + fmaf(c, xp, -pc));
   float e;
   float s = two_sum(d, -pb, e);
   t += e;
@@ -79,10 +83,23 @@ __device__ __forceinline__ float df_residual(float a, float b, float c, float d,
   t += e;
   s = two_sum(s, -pc, e);
   t += e;
+  return make_float2(s, t);
+}
+
+// The same for FP32 x, rounded to FP32.
+__device__ __forceinline__ float f_residual(float a, float b, float c, float d, float xm, float x0, float xp) {
+  const float2 st = residual_parts(a, b, c, d, xm, x0, xp);
+  return __fadd_rn(st.x, st.y);
+}
+
+// The same for double-float x (the low words' products added to t in FP32).
+__device__ __forceinline__ float df_residual(float a, float b, float c, float d, float2 xm, float2 x0, float2 xp) {
+  const float2 st = residual_parts(a, b, c, d, xm.x, x0.x, xp.x);
+  float t = st.y;
   t = fmaf(-b, x0.y, t);
   t = fmaf(-a, xm.y, t);
   t = fmaf(-c, xp.y, t);
-  return __fadd_rn(s, t);
+  return __fadd_rn(st.x, t);
 }
 
 }  // namespace tridi

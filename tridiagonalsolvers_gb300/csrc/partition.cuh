@@ -105,21 +105,36 @@ struct ChunkSummary {
   T lD, lC, lA;
 };
 
+// The right-hand side of row i as staged (rhs(i, a, b, c, d) = d).  A
+// right-hand side functor is told the chunk's first row (start) and then
+// called for the chunk's rows in order.
+struct RhsStaged {
+  __device__ __forceinline__ void start(int) const {}
+  template <class T>
+  __device__ __forceinline__ T operator()(int, T, T, T, T d) const {
+    return d;
+  }
+};
+
 // chunk_eliminate on rows held in shared memory (no size bound, K-free):
 // interior rows i < k-1 get (a, c, d) overwritten by (ap, cp, dp), so the
 // back substitution reads them again instead of holding 3k registers.
-template <class T>
+// Row i's right-hand side is rhs(i, a_i, b_i, c_i, d_i) of its staged values
+// (a correction solve forms its residual there, as the row is eliminated).
+template <class T, class Rhs = RhsStaged>
 __device__ __forceinline__ void chunk_eliminate_smem(ChunkSummary<T>& cs, int k, bool first, bool last,
                                                      T* __restrict__ sa, const T* __restrict__ sb,
-                                                     T* __restrict__ sc, T* __restrict__ sd) {
+                                                     T* __restrict__ sc, T* __restrict__ sd,
+                                                     const Rhs& rhs = Rhs()) {
   T cprev = T(0), aprev = T(0), dprev = T(0);
 #pragma unroll 4
   for (int i = 0; i < k - 1; ++i) {
-    const T a = (i == 0 && first) ? T(0) : sa[i];
-    const T inv = tdiv(T(1), sb[i] - a * cprev);
-    const T cn = sc[i] * inv;
+    const T a0 = sa[i], b0 = sb[i], c0 = sc[i];
+    const T a = (i == 0 && first) ? T(0) : a0;
+    const T inv = tdiv(T(1), b0 - a * cprev);
+    const T cn = c0 * inv;
     const T an = (i == 0 ? a : -a * aprev) * inv;
-    const T dn = (sd[i] - a * dprev) * inv;
+    const T dn = (rhs(i, a0, b0, c0, sd[i]) - a * dprev) * inv;
     sa[i] = an; sc[i] = cn; sd[i] = dn;
     cprev = cn; aprev = an; dprev = dn;
   }
@@ -138,7 +153,8 @@ __device__ __forceinline__ void chunk_eliminate_smem(ChunkSummary<T>& cs, int k,
     cs.lD = T(0); cs.lC = T(0); cs.lA = T(-1);
   }
   if (k >= 1) {
-    cs.sep = Row<T>{sa[k - 1], sb[k - 1], sc[k - 1], sd[k - 1]};
+    const T a0 = sa[k - 1], b0 = sb[k - 1], c0 = sc[k - 1];
+    cs.sep = Row<T>{a0, b0, c0, rhs(k - 1, a0, b0, c0, sd[k - 1])};
     if (k == 1 && first) cs.sep.a = T(0);
     if (last) cs.sep.c = T(0);
   } else {
@@ -164,6 +180,20 @@ __device__ __forceinline__ void chunk_back_smem(int k, T sj, T sl, const T* __re
   for (int i = k - 2; i >= 0; --i) {
     xn = sd[i] - sc[i] * xn - sa[i] * sl;
     emit(i, xn);
+  }
+}
+
+// Same, with x_i written over the chunk's d_i (row i's d is read once, by
+// the step that produces x_i).
+template <class T>
+__device__ __forceinline__ void chunk_back_smem_over_d(int k, T sj, T sl, const T* __restrict__ sa,
+                                                       const T* __restrict__ sc, T* __restrict__ sd) {
+  if (k >= 1) sd[k - 1] = sj;
+  T xn = sj;
+#pragma unroll 4
+  for (int i = k - 2; i >= 0; --i) {
+    xn = sd[i] - sc[i] * xn - sa[i] * sl;
+    sd[i] = xn;
   }
 }
 

@@ -36,16 +36,18 @@
 // Arithmetic: the partition solver of partition.cuh, per warp (MULTI), per
 // team of 160 threads (GROUP) or per CTA (SINGLE), with the chunk
 // elimination done in place in the ring (no register arrays, so no bound on
-// rows per thread) and the separators solved by PCR in shuffles (warp) or
-// shared memory (group, CTA).
+// rows per thread) and the separators solved by PCR in shuffles (warp), by
+// one warp of the team (group: a 5-row chunk per lane, then PCR in
+// shuffles), or by PCR in shared memory (CTA).
 //
 // Refined modes (tridi_ragged_refine_f32): every system is refined where it
 // sits, without leaving the SM: FP32 solve -> x; then `sweeps` times
-// { r = d - T x (extended precision; the original a, c, d are re-read from
-// L2 by the same loop and put back into the ring, where the FP32 elimination
-// had overwritten them); FP32 solve of T e = r in the ring; x += e (extended
-// precision) }; finally ||d - T x|| / ||d|| per system (its maximum over the
-// batch goes to one device word) and x is written once as FP64.  So HBM sees
+// { the original a, c, d re-staged from L2 into the ring, where the FP32
+// elimination had overwritten them; FP32 solve of T e = r in the ring, each
+// row's residual r = d - T x formed in extended precision as the row is
+// eliminated; x += e (extended precision) }; finally, after one more
+// re-staging, ||d - T x|| / ||d|| per system (its maximum over the batch goes
+// to one device word) and x is written once as FP64.  So HBM sees
 // each coefficient once and each unknown once (16 B in, 8 B out per row).
 // Extended precision is either native FP64 (RES_FP64) or double-float, an
 // unevaluated sum of two FP32 values with a 48-bit significand (RES_DF).
@@ -55,6 +57,7 @@
 // 16-byte aligned (the bulk copies read whole 16-byte groups).
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "dfloat.cuh"
@@ -73,6 +76,7 @@ constexpr int kSlots = 9;              // items in flight (descriptor slots), 3 
 constexpr int kWarpMaxRows = 480;      // MULTI systems by default: up to 15 rows per lane
 constexpr int kGroupMaxRows = 4800;    // GROUP systems by default: up to 30 rows per thread
 constexpr int kMaxItemSystems = kTeamWarps;  // 5
+static_assert(kTeamWarps & 1, "odd separator rows per lane in warp_solve_rows");
 static_assert(kTeams * kTeamWarps == kRagWarps && kSlots % kTeams == 0, "team shape");
 constexpr int kBigChunks = 3;                           // chunks per thread for BIG systems
 constexpr int kBigSepRows = kBigChunks * kRagThreads;   // chunks (separators) of a BIG system
@@ -82,7 +86,16 @@ constexpr int kBigScratchRows = 2 * kBigSepRows;        // ring rows a BIG item 
 
 // MULTI and GROUP items are a team's; SINGLE and BIG take the whole CTA.
 enum ItemKind : int { kMulti = 0, kGroup = 1, kSingle = 2, kBig = 3, kEnd = 4 };
-enum RagMode : int { kPlain = 0, kRefineDF = 1, kRefineFP64 = 2 };
+// Refined modes: kRefineDF / kRefineFP64 keep x in two extra ring arrays
+// (any number of sweeps); the one-correction modes kRefine1DF / kRefine1FP64
+// (sweeps == 1) keep the FP32 solution in the b words and the correction in
+// the d words, so their ring holds as many rows as the plain one.
+enum RagMode : int { kPlain = 0, kRefineDF = 1, kRefineFP64 = 2, kRefine1DF = 3, kRefine1FP64 = 4 };
+__host__ __device__ constexpr bool one_correction(int mode) { return mode >= kRefine1DF; }
+// DF or FP64: the residual arithmetic of a refined mode
+__host__ __device__ constexpr int residual_mode(int mode) {
+  return mode == kRefine1DF ? kRefineDF : (mode == kRefine1FP64 ? kRefineFP64 : mode);
+}
 
 // Shared-memory map: [head: 2 x kSlots mbarriers, kSlots descriptors]
 // [group scratch: kGroupFloats] [ring: ring_arrays(M) x ring_rows(M) floats].
@@ -90,7 +103,7 @@ constexpr int kHeadBytes = 1280;
 constexpr int kGroupFloats = 4 * kRagThreads + kRagThreads + 48 + 2 * 2 * kRagWarps + 4;  // R, X, F0, norms, max
 // (CTA-wide items use all of R, X, F0; team t uses its third of each.)
 constexpr int kSmemBudget = 232448;  // 227 KB, the opt-in maximum of sm_100-class GPUs
-__host__ __device__ constexpr int ring_arrays(int mode) { return mode == kPlain ? 4 : 6; }
+__host__ __device__ constexpr int ring_arrays(int mode) { return mode == kPlain || one_correction(mode) ? 4 : 6; }
 __host__ __device__ constexpr int ring_rows(int mode) {
   return ((kSmemBudget - kHeadBytes - 4 * kGroupFloats) / (4 * ring_arrays(mode))) & ~255;
 }
@@ -254,16 +267,49 @@ __device__ __forceinline__ void group_rel_max(float rr, float dd, int gt, int ba
 // barrier `bar` over the group): chunk elimination in place, the gt
 // separators solved by PCR (warp shuffles, or shared memory R: 4*gt floats,
 // X: gt, F0: 3*(gt/32)), back substitution; emit(i, x_i) for every row.
-template <class Emit>
+// Emit tag: x_i written over the ring's d_i.
+struct EmitOverD {};
+
+// The m = 32 q rows held in R (a, b, c, d at R, R + m, R + 2m, R + 3m; q
+// odd, so the lanes' strided accesses are conflict-free) solved by one warp
+// into X: lane l eliminates rows [l q, l q + q) in place, the 32 lane
+// separators are solved by PCR over shuffles, then each lane substitutes
+// back.  A team's separator system (m = 160) solved this way costs a few
+// hundred instructions of one warp instead of log2(m) barrier-separated PCR
+// steps of every thread of the team.
+__device__ __forceinline__ void warp_solve_rows(float* R, float* X, int m, int lane) {
+  const int q = m >> 5;
+  float* ra = R + lane * q;
+  float* rb = ra + m;
+  float* rc = rb + m;
+  float* rd = rc + m;
+  ChunkSummary<float> cs;
+  chunk_eliminate_smem<float>(cs, q, lane == 0, lane == 31, ra, rb, rc, rd);
+  const float nD = __shfl_down_sync(kFull, cs.fD, 1);
+  const float nC = __shfl_down_sync(kFull, cs.fC, 1);
+  const float nA = __shfl_down_sync(kFull, cs.fA, 1);
+  const float sj = warp_pcr32<float>(separator_row_s<float>(cs, nD, nC, nA));
+  float sl = __shfl_up_sync(kFull, sj, 1);
+  if (lane == 0) sl = 0.f;
+  float* xl = X + lane * q;
+  auto em = [&](int i, float v) { xl[i] = v; };
+  chunk_back_smem<float>(q, sj, sl, ra, rc, rd, em);
+}
+
+template <class Emit, class Rhs = RhsStaged>
 __device__ __forceinline__ void group_solve(int n, int gt, int bar, int gtid, float* sa, const float* sb, float* sc,
-                                            float* sd, float* R, float* X, float* F0, Emit& emit) {
+                                            float* sd, float* R, float* X, float* F0, Emit& emit,
+                                            const Rhs& rhs = Rhs()) {
   const int lane = gtid & 31, gw = gtid >> 5;
   const int kk = odd_ceil_dev((n + gt - 1) / gt);
   const int r0 = gtid * kk;
   int kr = n - r0;
   kr = kr < 0 ? 0 : (kr > kk ? kk : kr);
   ChunkSummary<float> cs;
-  chunk_eliminate_smem<float>(cs, kr, gtid == 0, r0 + kr == n && kr > 0, sa + r0, sb + r0, sc + r0, sd + r0);
+  rhs.start(r0);
+  const auto chunk_rhs = [&](int i, float a, float b, float c, float d) { return rhs(r0 + i, a, b, c, d); };
+  chunk_eliminate_smem<float>(cs, kr, gtid == 0, r0 + kr == n && kr > 0, sa + r0, sb + r0, sc + r0, sd + r0,
+                              chunk_rhs);
   float nD = __shfl_down_sync(kFull, cs.fD, 1);
   float nC = __shfl_down_sync(kFull, cs.fC, 1);
   float nA = __shfl_down_sync(kFull, cs.fA, 1);
@@ -281,26 +327,38 @@ __device__ __forceinline__ void group_solve(int n, int gt, int bar, int gtid, fl
       nD = F0[(gw + 1) * 3 + 0]; nC = F0[(gw + 1) * 3 + 1]; nA = F0[(gw + 1) * 3 + 2];
     }
     Row<float> sr = separator_row_s<float>(cs, nD, nC, nA);
-    const Row<float> id{0.f, 1.f, 0.f, 0.f};
-    for (int dl = 1; dl < gt; dl *= 2) {
+    if (gt <= kTeamThreads) {  // one warp solves the separators, the others wait at the barrier
       R[gtid] = sr.a; R[gt + gtid] = sr.b; R[2 * gt + gtid] = sr.c; R[3 * gt + gtid] = sr.d;
       group_sync(bar, gt);
-      const Row<float> L = gtid >= dl ? Row<float>{R[gtid - dl], R[gt + gtid - dl], R[2 * gt + gtid - dl],
-                                                   R[3 * gt + gtid - dl]}
-                                      : id;
-      const Row<float> Rr = gtid + dl < gt ? Row<float>{R[gtid + dl], R[gt + gtid + dl], R[2 * gt + gtid + dl],
-                                                        R[3 * gt + gtid + dl]}
-                                           : id;
-      sr = reduce_row(sr, L, Rr);
+      if (gw == 0) warp_solve_rows(R, X, gt, lane);
+      group_sync(bar, gt);
+      sj = X[gtid];
+    } else {  // the whole CTA: PCR, log2(gt) steps (shorter than one warp's chain over 15 rows per lane)
+      const Row<float> id{0.f, 1.f, 0.f, 0.f};
+      for (int dl = 1; dl < gt; dl *= 2) {
+        R[gtid] = sr.a; R[gt + gtid] = sr.b; R[2 * gt + gtid] = sr.c; R[3 * gt + gtid] = sr.d;
+        group_sync(bar, gt);
+        const Row<float> L = gtid >= dl ? Row<float>{R[gtid - dl], R[gt + gtid - dl], R[2 * gt + gtid - dl],
+                                                     R[3 * gt + gtid - dl]}
+                                        : id;
+        const Row<float> Rr = gtid + dl < gt ? Row<float>{R[gtid + dl], R[gt + gtid + dl], R[2 * gt + gtid + dl],
+                                                          R[3 * gt + gtid + dl]}
+                                             : id;
+        sr = reduce_row(sr, L, Rr);
+        group_sync(bar, gt);
+      }
+      sj = tdiv(sr.d, sr.b);
+      X[gtid] = sj;
       group_sync(bar, gt);
     }
-    sj = tdiv(sr.d, sr.b);
-    X[gtid] = sj;
-    group_sync(bar, gt);
     sl = gtid > 0 ? X[gtid - 1] : 0.f;
   }
-  auto em = [&](int i, float v) { emit(r0 + i, v); };
-  chunk_back_smem<float>(kr, sj, sl, sa + r0, sc + r0, sd + r0, em);
+  if constexpr (std::is_same_v<Emit, EmitOverD>) {
+    chunk_back_smem_over_d<float>(kr, sj, sl, sa + r0, sc + r0, sd + r0);
+  } else {
+    auto em = [&](int i, float v) { emit(r0 + i, v); };
+    chunk_back_smem<float>(kr, sj, sl, sa + r0, sc + r0, sd + r0, em);
+  }
   if (gt != 32) group_sync(bar, gt);  // F0 / R / X reused by the next solve
 }
 
@@ -332,6 +390,52 @@ struct EmitX {
   }
 };
 
+// Right-hand side of a correction solve: row i's residual d - (T x)_i, for
+// the rows of a chunk in order, x_{i-1} and x_i carried from the row before
+// (one x load per row).
+template <int MODE>
+struct RhsResidual;
+template <>
+struct RhsResidual<kRefineDF> {
+  XStore<kRefineDF> xs;
+  int n;
+  mutable float2 xm, x0;
+  __device__ __forceinline__ float2 at(int i) const {
+    return i >= 0 && i < n ? make_float2(xs.h[i], xs.l[i]) : make_float2(0.f, 0.f);
+  }
+  __device__ __forceinline__ void start(int i) const {
+    xm = at(i - 1);
+    x0 = at(i);
+  }
+  __device__ __forceinline__ float operator()(int i, float a, float b, float c, float d) const {
+    const float2 xp = at(i + 1);
+    const float r = df_residual(i > 0 ? a : 0.f, b, i < n - 1 ? c : 0.f, d, xm, x0, xp);
+    xm = x0;
+    x0 = xp;
+    return r;
+  }
+};
+template <>
+struct RhsResidual<kRefineFP64> {
+  XStore<kRefineFP64> xs;
+  int n;
+  mutable double xm, x0;
+  __device__ __forceinline__ double at(int i) const { return i >= 0 && i < n ? xs.get64(i) : 0.0; }
+  __device__ __forceinline__ void start(int i) const {
+    xm = at(i - 1);
+    x0 = at(i);
+  }
+  __device__ __forceinline__ float operator()(int i, float a, float b, float c, float d) const {
+    const double xp = at(i + 1);
+    double r = fma(-f2d_exact(b), x0, f2d_exact(d));
+    r = fma(-f2d_exact(i > 0 ? a : 0.f), xm, r);
+    r = fma(-f2d_exact(i < n - 1 ? c : 0.f), xp, r);
+    xm = x0;
+    x0 = xp;
+    return (float)r;
+  }
+};
+
 // The refinement's re-staging of a system's original a, c, d into its ring
 // slots (the FP32 elimination overwrote them there; b and the x words are
 // untouched): a bulk copy per array on the group's own mbarrier `mb`, whose
@@ -348,6 +452,7 @@ struct Restage {
   const float* src_c;
   const float* src_d;
   uint32_t bytes;
+  bool with_d;  // false: a and c only
 };
 
 __device__ __forceinline__ void restage(const Restage& rs, uint32_t& par, int gt, int bar, int gtid,
@@ -355,10 +460,10 @@ __device__ __forceinline__ void restage(const Restage& rs, uint32_t& par, int gt
   fence_proxy_async_smem();
   gsync(bar, gt);
   if (gtid == 0) {
-    mbar_arrive_expect_tx(rs.mb, 3u * rs.bytes);
+    mbar_arrive_expect_tx(rs.mb, (rs.with_d ? 3u : 2u) * rs.bytes);
     bulk_g2s(rs.dst_a, rs.src_a, rs.bytes, rs.mb);
     bulk_g2s(rs.dst_c, rs.src_c, rs.bytes, rs.mb);
-    bulk_g2s(rs.dst_d, rs.src_d, rs.bytes, rs.mb);
+    if (rs.with_d) bulk_g2s(rs.dst_d, rs.src_d, rs.bytes, rs.mb);
   }
   mbar_wait(rs.mb, (par >> rs.pbit) & 1u, status);
   par ^= 1u << rs.pbit;
@@ -366,8 +471,8 @@ __device__ __forceinline__ void restage(const Restage& rs, uint32_t& par, int gt
 
 // Refinement of one staged system by its solve group (see the file comment).
 // sa..sd: the system's rows in the ring, xh / xl: its x words in the ring.
-// Before each residual pass the originals are re-staged into the ring, so
-// the passes read shared memory only.
+// Before each correction solve and the final residual pass the originals are
+// re-staged into the ring, so the residuals read shared memory only.
 template <int MODE>
 __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& sy, int gt, int bar, int gtid,
                                              float* sa, const float* sb, float* sc, float* sd, float* xh, float* xl,
@@ -378,18 +483,14 @@ __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& s
   const long lo = sy.off & ~3L, hi = (sy.off + n + 3) & ~3L;
   const int pad = (int)(sy.off - lo);
   const Restage rs{mb, pbit, sa - pad, sc - pad, sd - pad, p.a + lo, p.c + lo, p.d + lo,
-                   (uint32_t)(4 * (hi - lo))};
-  for (int sw = -1; sw < p.sweeps; ++sw) {  // sw = -1: the first solve
-    if (sw >= 0) {
-      restage(rs, par, gt, bar, gtid, p.status);
-      for (int i = gtid; i < n; i += gt) {  // r overwrites d row by row; a, c stay for the solve
-        const float r = xs.residual(i, n, sa[i], sb[i], sc[i], sd[i]);
-        sd[i] = r;
-      }
-      gsync(bar, gt);
-    }
-    EmitX<MODE> em{xs, sw < 0};
-    group_solve(n, gt, bar, gtid, sa, sb, sc, sd, R, X, F0, em);
+                   (uint32_t)(4 * (hi - lo)), true};
+  EmitX<MODE> first{xs, true};
+  group_solve(n, gt, bar, gtid, sa, sb, sc, sd, R, X, F0, first);
+  for (int sw = 0; sw < p.sweeps; ++sw) {
+    // correction: the residual of each row formed as the row is eliminated
+    restage(rs, par, gt, bar, gtid, p.status);
+    EmitX<MODE> add{xs, false};
+    group_solve(n, gt, bar, gtid, sa, sb, sc, sd, R, X, F0, add, RhsResidual<MODE>{xs, n});
   }
   restage(rs, par, gt, bar, gtid, p.status);
   float rr = 0.f, dd = 0.f;
@@ -400,6 +501,117 @@ __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& s
     rr = fmaf(r, r, rr);
     dd = fmaf(d, d, dd);
     xo[i] = xs.get64(i);
+  }
+  group_rel_max(rr, dd, gt, bar, gtid, reinterpret_cast<float*>(red),
+                reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps));
+}
+
+// Right-hand side of the one-correction modes' correction solve: row i's
+// residual d - (T x0)_i for the FP32 solution x0 (held in the ring's b
+// words), rows of a chunk in order, x0_{i-1} and x0_i carried.
+template <int M>
+struct RhsResidual1 {
+  const float* x0w;
+  int n;
+  mutable float xm, x0;
+  __device__ __forceinline__ float at(int i) const { return i >= 0 && i < n ? x0w[i] : 0.f; }
+  __device__ __forceinline__ void start(int i) const {
+    xm = at(i - 1);
+    x0 = at(i);
+  }
+  __device__ __forceinline__ float operator()(int i, float a, float b, float c, float d) const {
+    const float xp = at(i + 1);
+    a = i > 0 ? a : 0.f;
+    c = i < n - 1 ? c : 0.f;
+    float r;
+    if constexpr (M == kRefineFP64) {
+      double v = fma(-f2d_exact(b), f2d_exact(x0), f2d_exact(d));
+      v = fma(-f2d_exact(a), f2d_exact(xm), v);
+      v = fma(-f2d_exact(c), f2d_exact(xp), v);
+      r = (float)v;
+    } else {
+      r = f_residual(a, b, c, d, xm, x0, xp);
+    }
+    xm = x0;
+    x0 = xp;
+    return r;
+  }
+};
+
+// One-correction refinement (sweeps == 1) of one staged system by its solve
+// group, in the ring's four arrays: the FP32 solve leaves x0 in the b words;
+// a, c, d are re-staged; the correction solve (b read from global memory,
+// each row's residual formed as the row is eliminated) leaves its solution e
+// in the d words; a and c are re-staged once more, and the final pass forms
+// d - T (x0 + e) with b and d from global memory, folds its norm into the
+// CTA's maximum and writes x0 + e as FP64.  M: kRefineDF or kRefineFP64.
+template <int M>
+__device__ __forceinline__ void group_refine1(const RagParams& p, const RagSys& sy, int gt, int bar, int gtid,
+                                              float* sa, float* sb, float* sc, float* sd, float* R, float* X,
+                                              float* F0, double* red, uint64_t* mb, int pbit, uint32_t& par) {
+  const int n = sy.n;
+  const long lo = sy.off & ~3L, hi = (sy.off + n + 3) & ~3L;
+  const int pad = (int)(sy.off - lo);
+  const uint32_t bytes = (uint32_t)(4 * (hi - lo));
+  const float* gb = p.b + sy.off;
+  const float* gd = p.d + sy.off;
+  EmitStore to_b{sb};
+  group_solve(n, gt, bar, gtid, sa, sb, sc, sd, R, X, F0, to_b);
+  restage(Restage{mb, pbit, sa - pad, sc - pad, sd - pad, p.a + lo, p.c + lo, p.d + lo, bytes, true}, par, gt, bar,
+          gtid, p.status);
+  EmitOverD to_d;
+  group_solve(n, gt, bar, gtid, sa, gb, sc, sd, R, X, F0, to_d, RhsResidual1<M>{sb, n});
+  // The final pass reads b and d from global memory (L2): each thread keeps
+  // the loads of its next kAhead rows in flight, the first ones issued
+  // before the re-staging wait.
+  constexpr int kAhead = 4;
+  float nb[kAhead], nd[kAhead];
+#pragma unroll
+  for (int q = 0; q < kAhead; ++q) {
+    const int j = gtid + q * gt;
+    nb[q] = j < n ? gb[j] : 0.f;
+    nd[q] = j < n ? gd[j] : 0.f;
+  }
+  restage(Restage{mb, pbit, sa - pad, sc - pad, sd - pad, p.a + lo, p.c + lo, p.d + lo, bytes, false}, par, gt, bar,
+          gtid, p.status);
+  float rr = 0.f, dd = 0.f;
+  double* xo = p.x64 + sy.off;
+  for (int i0 = gtid; i0 < n; i0 += kAhead * gt) {
+#pragma unroll
+    for (int q = 0; q < kAhead; ++q) {
+      const int i = i0 + q * gt;
+      if (i >= n) break;
+      const float b = nb[q], d = nd[q];
+      const int j = i + kAhead * gt;
+      if (j < n) {
+        nb[q] = gb[j];
+        nd[q] = gd[j];
+      }
+      const float a = i > 0 ? sa[i] : 0.f, c = i < n - 1 ? sc[i] : 0.f;
+      // x = x0 + e: the pair's low word is within a few ulps of the high one
+      const float2 xm = i > 0 ? make_float2(sb[i - 1], sd[i - 1]) : make_float2(0.f, 0.f);
+      const float2 x0 = make_float2(sb[i], sd[i]);
+      const float2 xp = i < n - 1 ? make_float2(sb[i + 1], sd[i + 1]) : make_float2(0.f, 0.f);
+      float r;
+      if constexpr (M == kRefineFP64) {
+        const auto x64 = [](float2 v) {
+          float l;
+          const float h = two_sum(v.x, v.y, l);
+          return df_to_double(h, l);
+        };
+        double v = fma(-f2d_exact(b), x64(x0), f2d_exact(d));
+        v = fma(-f2d_exact(a), x64(xm), v);
+        v = fma(-f2d_exact(c), x64(xp), v);
+        r = (float)v;
+      } else {
+        r = df_residual(a, b, c, d, xm, x0, xp);
+      }
+      rr = fmaf(r, r, rr);
+      dd = fmaf(d, d, dd);
+      float l;
+      const float h = two_sum(x0.x, x0.y, l);
+      xo[i] = df_to_double(h, l);
+    }
   }
   group_rel_max(rr, dd, gt, bar, gtid, reinterpret_cast<float*>(red),
                 reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps));
@@ -683,6 +895,9 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
         if constexpr (MODE == kPlain) {
           group_solve_plain(sy.n, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, Rsh, Xsh, F0,
                             p.x + sy.off);
+        } else if constexpr (one_correction(MODE)) {
+          group_refine1<residual_mode(MODE)>(p, sy, kRagThreads, 1, tid, A + base, B + base, C + base, D + base,
+                                             Rsh, Xsh, F0, red, &rbar[kRagWarps + kTeams], kRagWarps + kTeams, rpar);
         } else {
           group_refine<MODE>(p, sy, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, XH + base, XL + base,
                              Rsh, Xsh, F0, red, &rbar[kRagWarps + kTeams], kRagWarps + kTeams, rpar);
@@ -698,8 +913,8 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
           solve_big(sy, p.a + sy.off, p.b + sy.off, p.c + sy.off, p.d + sy.off, tid, Ra, Rb, Rc, Rd,
                     Ra + kBigSepRows, Rb + kBigSepRows, Rc + kBigSepRows, Rd + kBigSepRows, em);
         } else {
-          big_refine<MODE>(p, sy, tid, Ra, Rb, Rc, Rd, Ra + kBigSepRows, Rb + kBigSepRows, Rc + kBigSepRows,
-                           Rd + kBigSepRows, red);
+          big_refine<residual_mode(MODE)>(p, sy, tid, Ra, Rb, Rc, Rd, Ra + kBigSepRows, Rb + kBigSepRows,
+                                          Rc + kBigSepRows, Rd + kBigSepRows, red);
         }
       }
       release_stage(&empty[s]);
@@ -723,6 +938,9 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
           if constexpr (MODE == kPlain) {
             group_solve_plain(sy.n, 32, 0, lane, A + base, B + base, C + base, D + base, nullptr, nullptr, nullptr,
                               p.x + sy.off);
+          } else if constexpr (one_correction(MODE)) {
+            group_refine1<residual_mode(MODE)>(p, sy, 32, 0, lane, A + base, B + base, C + base, D + base, nullptr,
+                                               nullptr, nullptr, red, &rbar[warp], warp, rpar);
           } else {
             group_refine<MODE>(p, sy, 32, 0, lane, A + base, B + base, C + base, D + base, XH + base, XL + base,
                                nullptr, nullptr, nullptr, red, &rbar[warp], warp, rpar);
@@ -734,6 +952,9 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
         if constexpr (MODE == kPlain) {
           group_solve_plain(sy.n, kTeamThreads, tbar, ttid, A + base, B + base, C + base, D + base, tR, tX, tF,
                             p.x + sy.off);
+        } else if constexpr (one_correction(MODE)) {
+          group_refine1<residual_mode(MODE)>(p, sy, kTeamThreads, tbar, ttid, A + base, B + base, C + base, D + base,
+                                             tR, tX, tF, red, &rbar[kRagWarps + team], kRagWarps + team, rpar);
         } else {
           group_refine<MODE>(p, sy, kTeamThreads, tbar, ttid, A + base, B + base, C + base, D + base, XH + base,
                              XL + base, tR, tX, tF, red, &rbar[kRagWarps + team], kRagWarps + team, rpar);
@@ -1008,9 +1229,11 @@ tridi_status tridi_ragged_refine_f32(const float* a, const float* b, const float
   p.rel = reinterpret_cast<unsigned long long*>(dev_rel);
   p.sweeps = sweeps;
   const int res = tunable(TRIDI_TUNE_RESIDUAL);
-  if (res == TRIDI_RESIDUAL_FP64) return ragged_launch<kRefineFP64>(plan, dev_plan, p, st);
-  if (res != 0 && res != TRIDI_RESIDUAL_DF) return TRIDI_ERROR_INVALID_VALUE;
-  return ragged_launch<kRefineDF>(plan, dev_plan, p, st);
+  if (res != 0 && res != TRIDI_RESIDUAL_DF && res != TRIDI_RESIDUAL_FP64) return TRIDI_ERROR_INVALID_VALUE;
+  const bool fp64 = res == TRIDI_RESIDUAL_FP64;
+  if (sweeps == 1)  // x0 and its correction in the ring's b and d words
+    return fp64 ? ragged_launch<kRefine1FP64>(plan, dev_plan, p, st) : ragged_launch<kRefine1DF>(plan, dev_plan, p, st);
+  return fp64 ? ragged_launch<kRefineFP64>(plan, dev_plan, p, st) : ragged_launch<kRefineDF>(plan, dev_plan, p, st);
 }
 
 }  // extern "C"
