@@ -75,6 +75,8 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
 #define TRIDI_SERVER_COPY_DIRECT 2 /*   2 = kernels read / write the callers' arrays (pageable memory access); */
 #define TRIDI_SERVER_COPY_STAGED 3 /*   0 or 3 = pinned double-buffered staging filled by host threads */
 #define TRIDI_TUNE_LARGE_TMA 6    /* interleaved FP32 large systems: 0/1 = TMA-tiled passes where they apply, 2 = off */
+#define TRIDI_TUNE_WARP_STREAMS 7 /* CR/PCR/CR-PCR with a system per warp or less: 0/1 = every warp streams its own
+                                     systems (no producer warp), 2 = CTA ring filled by a producer warp */
 tridi_status tridi_set_tunable(int key, int value);
 int tridi_get_tunable(int key);
 

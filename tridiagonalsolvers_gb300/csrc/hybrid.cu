@@ -46,6 +46,28 @@ bool choose_shape(int n, Shape* s) {
 constexpr int kWarpThreads = 128 + 32;   // 4 consumer warps + producer warp
 constexpr int kBlockThreads = 256 + 32;  // up to 8 consumer warps + producer
 
+// Warp shapes with bulk-copy alignment: hybrid_warp_kernel, two buffers per
+// warp, as many CTAs of 4 warps as registers and shared memory allow.
+template <class T, int K, int LSTRIDE>
+cudaError_t launch_warp_streams(const HybridParams& p, const DeviceInfo& dev, cudaStream_t stream) {
+  constexpr int MINB = K >= 16 ? 4 : 5;  // 5: at most 96 registers, 20 warps per SM
+  auto kern = hybrid_warp_kernel<T, K, LSTRIDE, MINB>;
+  const int warps = kWarpKernelThreads / 32;
+  const size_t smem = HybridSmem<T>::barrier_bytes() + (size_t)warps * 2 * HybridSmem<T>::stage_elems(32 / p.tps, p.n) * sizeof(T);
+  if (smem > (size_t)dev.max_smem_optin) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarpKernelThreads, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  const long tiles = ((long)p.m + 32 / p.tps - 1) / (32 / p.tps);
+  long grid = (long)per_sm * dev.sm_count;
+  if (grid * warps > tiles) grid = (tiles + warps - 1) / warps;
+  kern<<<(unsigned)grid, kWarpKernelThreads, smem, stream>>>(p);
+  return cudaGetLastError();
+}
+
 template <class T, int K, bool WARP, int LSTRIDE>
 cudaError_t launch_one(const HybridParams& p0, const DeviceInfo& dev, cudaStream_t stream) {
   constexpr int MAXT = WARP ? kWarpThreads : kBlockThreads;
@@ -54,6 +76,11 @@ cudaError_t launch_one(const HybridParams& p0, const DeviceInfo& dev, cudaStream
   HybridParams p = p0;
   const bool tma_ok = aligned16(p.a) && aligned16(p.b) && aligned16(p.c) && aligned16(p.d) && aligned16(p.x) &&
                       ((size_t)p.n * sizeof(T)) % 16 == 0;
+  // (FP32 shapes that keep their registers at 20 warps per SM; the FP64
+  // shapes and PCR on 16 rows per thread would spill)
+  if constexpr (WARP && sizeof(T) == 4 && !(K == 16 && LSTRIDE == 1)) {
+    if (tma_ok && tunable(TRIDI_TUNE_WARP_STREAMS) != 2) return launch_warp_streams<T, K, LSTRIDE>(p, dev, stream);
+  }
   const int logk = Log2<K>::value;
   const size_t stage_bytes = HybridSmem<T>::stage_elems(p.G, p.n) * sizeof(T);
   const size_t fixed = HybridSmem<T>::bytes(0, p.G, p.n, p.scratch_rows, WARP, p.ct, logk);

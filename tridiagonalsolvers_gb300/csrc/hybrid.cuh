@@ -362,6 +362,8 @@ struct HybridSmem {
   }
 };
 
+constexpr int kWarpKernelThreads = 128;  // hybrid_warp_kernel: 4 warps per CTA
+
 template <class T, int K, bool WARP, int LSTRIDE, int MAXT, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB) hybrid_kernel(HybridParams p) {
   constexpr int LOGK = Log2<K>::value;
@@ -467,6 +469,76 @@ __global__ void __launch_bounds__(MAXT, MINB) hybrid_kernel(HybridParams p) {
     }
   }
   (void)LOGK;
+}
+
+// Warp shapes (a system's group fits in one warp) without a producer warp:
+// every warp streams its own systems through a private two-buffer ring.
+// While a warp solves warp tile k (32 / tps systems, loaded from its buffer
+// into registers), the bulk copies of its next tile fill the other buffer.
+// No CTA barrier and no producer warp: all resident warps solve, so more of
+// them fit an SM at the same register budget.  Needs the bulk-copy
+// alignment (16-byte pointers, n * sizeof(T) a multiple of 16).
+template <class T, int K, int LSTRIDE, int MINB>
+__global__ void __launch_bounds__(kWarpKernelThreads, MINB) hybrid_warp_kernel(HybridParams p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = p.n, tps = p.tps;
+  const int gw = 32 / tps;  // systems per warp tile
+  const size_t buf_elems = (size_t)4 * gw * n;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + 2 * warp;
+  T* buf = reinterpret_cast<T*>(smem + HybridSmem<T>::barrier_bytes()) + (size_t)2 * warp * buf_elems;
+  const T* ga = static_cast<const T*>(p.a);
+  const T* gb = static_cast<const T*>(p.b);
+  const T* gc = static_cast<const T*>(p.c);
+  const T* gd = static_cast<const T*>(p.d);
+  T* gx = static_cast<T*>(p.x);
+  const long tiles = ((long)p.m + gw - 1) / gw;
+  const long first = (long)blockIdx.x * (blockDim.x >> 5) + warp;
+  const long step = (long)gridDim.x * (blockDim.x >> 5);
+  if (lane == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_fence_init();
+  }
+  __syncwarp();
+  const auto issue = [&](long tile, int s) {  // lane 0
+    const long sys0 = tile * gw;
+    const long ns = (p.m - sys0) < gw ? (p.m - sys0) : gw;
+    const uint32_t bytes = (uint32_t)(ns * n * sizeof(T));
+    T* st = buf + s * buf_elems;
+    mbar_arrive_expect_tx(&bars[s], 4 * bytes);
+    bulk_g2s(st + 0 * (size_t)gw * n, ga + sys0 * n, bytes, &bars[s]);
+    bulk_g2s(st + 1 * (size_t)gw * n, gb + sys0 * n, bytes, &bars[s]);
+    bulk_g2s(st + 2 * (size_t)gw * n, gc + sys0 * n, bytes, &bars[s]);
+    bulk_g2s(st + 3 * (size_t)gw * n, gd + sys0 * n, bytes, &bars[s]);
+  };
+  if (lane == 0 && first < tiles) issue(first, 0);
+  const int g = lane / tps, t = lane - g * tps;
+  int k = 0;
+  for (long tile = first; tile < tiles; tile += step, ++k) {
+    const int s = k & 1;
+    // the other buffer was read into registers one tile ago (and the warp
+    // synchronised since): refill it with the next tile
+    if (lane == 0 && tile + step < tiles) {
+      fence_proxy_async_smem();
+      issue(tile + step, s ^ 1);
+    }
+    if (!mbar_wait(&bars[s], (k >> 1) & 1, p.status)) break;
+    const T* st = buf + s * buf_elems + (size_t)g * n + (size_t)t * K;
+    T va[K], vb[K], vc[K], vd[K];
+    load_vec_smem<T, K>(st + 0 * (size_t)gw * n, va);
+    load_vec_smem<T, K>(st + 1 * (size_t)gw * n, vb);
+    load_vec_smem<T, K>(st + 2 * (size_t)gw * n, vc);
+    load_vec_smem<T, K>(st + 3 * (size_t)gw * n, vd);
+    __syncwarp();
+    Row<T> r[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) r[i] = Row<T>{va[i], vb[i], vc[i], vd[i]};
+    T xr[K];
+    hybrid_solve<T, K, true, LSTRIDE>(r, xr, t, tps, p.stride, GroupScratch<T>{}, nullptr, 32);
+    const long sys = tile * gw + g;
+    if (sys < p.m) store_vec<T, K>(gx + sys * n + (long)t * K, xr);
+  }
 }
 
 }  // namespace tridi
