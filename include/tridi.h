@@ -77,6 +77,9 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
 #define TRIDI_TUNE_LARGE_TMA 6    /* interleaved FP32 large systems: 0/1 = TMA-tiled passes where they apply, 2 = off */
 #define TRIDI_TUNE_WARP_STREAMS 7 /* CR/PCR/CR-PCR with a system per warp or less: 0/1 = every warp streams its own
                                      systems (no producer warp), 2 = CTA ring filled by a producer warp */
+#define TRIDI_TUNE_NBC_KERNEL 8   /* bank-conflict-free CR: 0/1 = the register kernel where it has the shape
+                                     (same arithmetic and results, about twice as fast), 2 = the
+                                     shared-memory kernel always */
 tridi_status tridi_set_tunable(int key, int value);
 int tridi_get_tunable(int key);
 
@@ -103,16 +106,23 @@ tridi_status tridi_crpcr_f32(const float *a, const float *b, const float *c, con
 tridi_status tridi_crpcr_f64(const double *a, const double *b, const double *c, const double *d, double *x,
                              int n, int num_systems, int rest_system_size, tridi_stream_t stream);
 
-/* Bank-conflict-free shared-memory cyclic reduction.  Replaces crNBC()
-   (crNBC.cu:123 / crNBCKernel :20) and crNBC32() (crNBC32banks.cu:123 /
-   crNBC32Kernel :20).  n a power of two, 2 <= n <= 2048. */
+/* Bank-conflict-free cyclic reduction.  Replaces crNBC() (crNBC.cu:123 /
+   crNBCKernel :20) and crNBC32() (crNBC32banks.cu:123 / crNBC32Kernel :20).
+   n a power of two, 2 <= n <= 4096 (FP64: 2048).  Two kernels with the same
+   arithmetic and bit-identical results: the register CR of tridi_cr_* (rows
+   in registers, the staging ring read with conflict-free 16-byte loads; used
+   by default) and a shared-memory CR whose every level is conflict-free by
+   construction (each level compacted into a dense array; the last 32-row
+   levels in registers), selected with TRIDI_TUNE_NBC_KERNEL = 2. */
 tridi_status tridi_cr_nbc_f32(const float *a, const float *b, const float *c, const float *d, float *x, int n,
                               int num_systems, tridi_stream_t stream);
 tridi_status tridi_cr_nbc_f64(const double *a, const double *b, const double *c, const double *d, double *x,
                               int n, int num_systems, tridi_stream_t stream);
 
 /* Hybrid with the bank-conflict-free CR part.  Replaces crpcrNBC()
-   (crNBC.cu:344 / crpcrNBCKernel :189). */
+   (crNBC.cu:344 / crpcrNBCKernel :189).  Kernel choice as for tridi_cr_nbc_*:
+   the register CR-PCR of tridi_crpcr_* by default, the shared-memory one with
+   TRIDI_TUNE_NBC_KERNEL = 2. */
 tridi_status tridi_crpcr_nbc_f32(const float *a, const float *b, const float *c, const float *d, float *x,
                                  int n, int num_systems, int rest_system_size, tridi_stream_t stream);
 tridi_status tridi_crpcr_nbc_f64(const double *a, const double *b, const double *c, const double *d,

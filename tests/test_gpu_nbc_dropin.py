@@ -39,6 +39,46 @@ def test_cr_nbc_vs_oracle(cuda, n, prec):
         check_ulps(x, xr, ulps=4)
 
 
+TUNE_NBC_KERNEL = 8  # tridi.h: TRIDI_TUNE_NBC_KERNEL (2 = the shared-memory kernel)
+
+
+@pytest.fixture
+def shared_memory_kernel():
+    from tridiagonalsolvers_gb300 import _lib
+
+    L = _lib.lib()
+    _lib.check(L.tridi_set_tunable(TUNE_NBC_KERNEL, 2), "tridi_set_tunable")
+    yield
+    L.tridi_set_tunable(TUNE_NBC_KERNEL, 0)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("n", [2, 4, 32, 64, 256, 1024, 2048])
+def test_shared_memory_kernel_matches_register_cr(cuda, shared_memory_kernel, n, prec):
+    """The shared-memory CR (compacted levels, register tail) against the FP64
+    oracle, and bit for bit against the register CR: the same arithmetic."""
+    dt = NP[prec]
+    for m in (1, 33):
+        a, b, c, d = workloads.dominant(m, n, seed=500 + n + m, dtype=dt)
+        t = _dev(cuda, a, b, c, d)
+        x = tg.crNBC(*t).cpu().numpy()
+        assert tg.device_status() == 0
+        check_against_oracle(a, b, c, d, x, dtype=dt)
+        assert np.array_equal(x, tg.cr(*t).cpu().numpy())
+
+
+@pytest.mark.parametrize("n", [8, 64, 256])
+def test_shared_memory_crpcr_sweep(cuda, shared_memory_kernel, n):
+    a, b, c, d = workloads.dominant(19, n, seed=27 + n)
+    t = _dev(cuda, a, b, c, d)
+    rest = 2
+    while rest <= n // 2:
+        x = tg.crpcrNBC(*t, rest).cpu().numpy()
+        check_against_oracle(a, b, c, d, x)
+        check_ulps(x, tg.crpcr(*t, rest_system_size=rest).cpu().numpy())
+        rest *= 2
+
+
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 @pytest.mark.parametrize("n", [8, 64, 256, 1024])
 def test_crpcr_nbc_sweep(cuda, n, prec):

@@ -1,6 +1,10 @@
-// Launch logic and C-ABI entry points of the bank-conflict-free shared-memory
-// CR (nbc.cuh).  Replaces the device work of crNBC() (crNBC.cu:123),
-// crNBC32() (crNBC32banks.cu:123) and crpcrNBC() (crNBC.cu:344).
+// Launch logic and C-ABI entry points of the bank-conflict-free CR: the
+// register kernels of hybrid.cu by default (the same arithmetic, results
+// bit-identical to the shared-memory kernel, about twice its speed), the
+// shared-memory CR of nbc.cuh on request (TRIDI_TUNE_NBC_KERNEL = 2) or where
+// the register kernel has no shape.  Replaces the device work of crNBC()
+// (crNBC.cu:123), crNBC32() (crNBC32banks.cu:123) and crpcrNBC()
+// (crNBC.cu:344).
 #include "nbc.cuh"
 #include "runtime.h"
 
@@ -17,6 +21,16 @@ tridi_status solve_nbc(const T* a, const T* b, const T* c, const T* d, T* x, int
   const int nmax = sizeof(T) == 4 ? 4096 : 2048;
   if (!is_pow2(n) || n < 2 || n > nmax) return TRIDI_ERROR_UNSUPPORTED_SIZE;
   if (!is_pow2(rest) || rest < 2 || rest > (n > 2 ? n / 2 : 2)) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  if (tunable(TRIDI_TUNE_NBC_KERNEL) != 2) {
+    // the register kernels: the same arithmetic (bit-identical results), no
+    // shared-memory bank traffic but conflict-free 16-byte loads of the ring
+    tridi_status st;
+    if constexpr (sizeof(T) == 4)
+      st = rest == 2 ? tridi_cr_f32(a, b, c, d, x, n, m, stream) : tridi_crpcr_f32(a, b, c, d, x, n, m, rest, stream);
+    else
+      st = rest == 2 ? tridi_cr_f64(a, b, c, d, x, n, m, stream) : tridi_crpcr_f64(a, b, c, d, x, n, m, rest, stream);
+    if (st != TRIDI_ERROR_UNSUPPORTED_SIZE) return st;
+  }
   const DeviceInfo* dev = current_device();
   if (!dev) return TRIDI_ERROR_CUDA;
 
@@ -47,7 +61,7 @@ tridi_status solve_nbc(const T* a, const T* b, const T* c, const T* d, T* x, int
   p.stages = S;
   p.ntiles = (int)(((long)m + G - 1) / G);
   const size_t smem = NbcSmem<T>::bytes(S, G, n, rest);
-  auto kern = nbc_kernel<T, kMaxThreads>;
+  auto kern = nbc_kernel<T, kMaxThreads, sizeof(T) == 4 ? 5 : 1>;  // FP32: 5 CTAs (20 solving warps) per SM
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e);
   const int threads = 32 * G + 32;

@@ -78,6 +78,35 @@ __device__ __forceinline__ void store_pair(T* p, int i, T lo, T hi, bool vec) {
   }
 }
 
+// The last CR levels of one system in registers: the level's nl <= 32 rows
+// (ca..cd) one per lane, the rows (t + 1) % 2D == 0 reduced against the rows
+// D away over shuffles until two remain, their 2x2 solve, then back
+// substitution the same way; x of the level's rows lands in xo.  The same
+// formulas in the same order as the shared-memory levels (the odd rows of
+// one level are the rows (t + 1) % 2D == 0 of the next finer spacing).
+template <class T>
+__device__ __forceinline__ void register_tail(const T* ca, const T* cb, const T* cc, const T* cd, T* xo, int nl,
+                                              int lane) {
+  const int t = lane;
+  Row<T> C = t < nl ? Row<T>{ca[t], cb[t], cc[t], cd[t]} : Row<T>{T(0), T(1), T(0), T(0)};
+  for (int D = 1; 2 * D < nl; D *= 2) {
+    const Row<T> L = shfl_up(C, D, 32);
+    Row<T> R = shfl_down(C, D, 32);
+    if (t == nl - 1) R = C;  // right neighbour clamped to the last row (cr_kernel.cu:52)
+    if (t < nl && ((t + 1) & (2 * D - 1)) == 0) C = reduce_row(C, L, R);
+  }
+  T xC = T(0);
+  const Row<T> pr = shfl_xor(C, nl / 2, 32);
+  if (t == nl / 2 - 1) xC = solve2_upper(C, pr);
+  if (t == nl - 1) xC = solve2_lower(pr, C);
+  for (int D = nl / 4; D >= 1; D /= 2) {
+    const T xl = __shfl_up_sync(kFull, xC, D);
+    const T xr = __shfl_down_sync(kFull, xC, D);
+    if (t < nl && ((t + 1) & (2 * D - 1)) == D) xC = back_row(C, xl, xr, t == D - 1);
+  }
+  if (t < nl) xo[t] = xC;
+}
+
 // One system, one warp.  (la, lb, lc, ld): level-0 arrays (shared stage or
 // global); W: the warp's working area; xg: the system's x in global memory.
 template <class T>
@@ -92,17 +121,31 @@ __device__ void nbc_solve(const T* la, const T* lb, const T* lc, const T* ld, T*
   T* P = W + 5 * n;  // PCR ping-pong, 4 * rest
 
   // ---- forward CR levels: level l (nl rows) -> level l+1 (nl/2 rows) ----
+  // Plain CR (rest == 2) leaves the shared-memory levels at 32 rows: one row
+  // per lane, the remaining levels in registers (register_tail).
+  const int stop = rest == 2 ? 32 : rest;
   const T *sa = la, *sb = lb, *sc = lc, *sd = ld;
   bool svec = vec0;
   int nl = n;
-  while (nl > rest) {
+  while (nl > stop) {
     const int half = nl / 2;
     const int off = n - nl;  // offset of level l+1 (n - 2 * (nl/2))
+    // level l is read, level l+1 written: disjoint arrays, so the iterations'
+    // loads may run ahead of the previous iterations' stores
+    const T* __restrict__ ra = sa;
+    const T* __restrict__ rb = sb;
+    const T* __restrict__ rc = sc;
+    const T* __restrict__ rd = sd;
+    T* __restrict__ wa = A + off;
+    T* __restrict__ wb = B + off;
+    T* __restrict__ wc = C + off;
+    T* __restrict__ wd = D + off;
+#pragma unroll 2
     for (int j0 = 0; j0 < half; j0 += 32) {
       const int j = j0 + lane;
       const int jj = j < half ? j : half - 1;
-      const Pair<T> pa = load_pair(sa, 2 * jj, svec), pb = load_pair(sb, 2 * jj, svec),
-                    pc = load_pair(sc, 2 * jj, svec), pd = load_pair(sd, 2 * jj, svec);
+      const Pair<T> pa = load_pair(ra, 2 * jj, svec), pb = load_pair(rb, 2 * jj, svec),
+                    pc = load_pair(rc, 2 * jj, svec), pd = load_pair(rd, 2 * jj, svec);
       Row<T> R{__shfl_down_sync(kFull, pa.lo, 1), __shfl_down_sync(kFull, pb.lo, 1),
                __shfl_down_sync(kFull, pc.lo, 1), __shfl_down_sync(kFull, pd.lo, 1)};
       const Row<T> me{pa.hi, pb.hi, pc.hi, pd.hi};
@@ -110,11 +153,11 @@ __device__ void nbc_solve(const T* la, const T* lb, const T* lc, const T* ld, T*
         R = me;  // right neighbour clamped to the last row (cr_kernel.cu:52)
       } else if (lane == 31) {
         const int k = 2 * jj + 2;
-        R = Row<T>{sa[k], sb[k], sc[k], sd[k]};
+        R = Row<T>{ra[k], rb[k], rc[k], rd[k]};
       }
       const Row<T> o = reduce_row(me, Row<T>{pa.lo, pb.lo, pc.lo, pd.lo}, R);
       if (j < half) {
-        A[off + j] = o.a; B[off + j] = o.b; C[off + j] = o.c; D[off + j] = o.d;
+        wa[j] = o.a; wb[j] = o.b; wc[j] = o.c; wd[j] = o.d;
       }
     }
     __syncwarp();
@@ -123,9 +166,11 @@ __device__ void nbc_solve(const T* la, const T* lb, const T* lc, const T* ld, T*
     nl = half;
   }
 
-  // ---- the intermediate system (nl == rest rows): PCR, then 2x2 pairs ----
   T* xl = (nl == n) ? nullptr : X + (n - 2 * nl);  // x of the intermediate level
-  {
+  if (rest == 2) {
+    register_tail<T>(sa, sb, sc, sd, xl ? xl : xg, nl, lane);
+  } else {
+  // ---- the intermediate system (nl == rest rows): PCR, then 2x2 pairs ----
     const T *ca = sa, *cb = sb, *cc = sc, *cd = sd;
     T *pa = P, *pb = P + rest, *pc = P + 2 * rest, *pd = P + 3 * rest;
     T *qa = const_cast<T*>(sa), *qb = const_cast<T*>(sb), *qc = const_cast<T*>(sc), *qd = const_cast<T*>(sd);
@@ -156,8 +201,8 @@ __device__ void nbc_solve(const T* la, const T* lb, const T* lc, const T* ld, T*
         xg[j + h] = x2;
       }
     }
-    __syncwarp();
   }
+  __syncwarp();
 
   // ---- back substitution: level l+1 x -> level l x, down to level 0 ----
   while (nl < n) {
@@ -170,9 +215,11 @@ __device__ void nbc_solve(const T* la, const T* lb, const T* lc, const T* ld, T*
       const int o = n - 2 * nu;
       ra = A + o; rb = B + o; rc = C + o; rd = D + o; rvec = true;
     }
-    const T* xo_arr = X + (n - 2 * nl);  // x of level l+1 (odd rows of level l)
-    T* xe_arr = (nu == n) ? xg : X + (n - 2 * nu);
+    // x of level l+1 (odd rows of level l) is read, x of level l written
+    const T* __restrict__ xo_arr = X + (n - 2 * nl);
+    T* __restrict__ xe_arr = (nu == n) ? xg : X + (n - 2 * nu);
     const bool xvec = (nu == n) ? vecx : true;
+#pragma unroll 2
     for (int j0 = 0; j0 < nl; j0 += 32) {
       const int j = j0 + lane;
       const int jj = j < nl ? j : nl - 1;
@@ -189,8 +236,8 @@ __device__ void nbc_solve(const T* la, const T* lb, const T* lc, const T* ld, T*
   }
 }
 
-template <class T, int MAXT>
-__global__ void __launch_bounds__(MAXT) nbc_kernel(NbcParams p) {
+template <class T, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) nbc_kernel(NbcParams p) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + 8;
