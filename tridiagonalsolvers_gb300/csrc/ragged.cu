@@ -107,6 +107,9 @@ __host__ __device__ constexpr int ring_arrays(int mode) { return mode == kPlain 
 __host__ __device__ constexpr int ring_rows(int mode) {
   return ((kSmemBudget - kHeadBytes - 4 * kGroupFloats) / (4 * ring_arrays(mode))) & ~255;
 }
+// The ring is the destination of bulk copies: its start (and every array's)
+// must be 16-byte aligned.
+static_assert((kHeadBytes + 4 * kGroupFloats) % 16 == 0, "ring start 16-byte aligned");
 constexpr size_t rag_smem_bytes(int mode) {
   return (size_t)kHeadBytes + 4 * (size_t)kGroupFloats + 4 * (size_t)ring_arrays(mode) * ring_rows(mode);
 }
