@@ -68,6 +68,26 @@ cudaError_t launch_warp_streams(const HybridParams& p, const DeviceInfo& dev, cu
   return cudaGetLastError();
 }
 
+// Block shapes with one 128-thread CTA of groups (tps 64 or 128) and
+// bulk-copy alignment: hybrid_block_stream_kernel, no producer warp.
+template <class T, int K, int LSTRIDE>
+cudaError_t launch_block_streams(const HybridParams& p, const DeviceInfo& dev, cudaStream_t stream) {
+  constexpr int MINB = K >= 16 ? 4 : 5;
+  auto kern = hybrid_block_stream_kernel<T, K, LSTRIDE, 128, MINB>;
+  const size_t smem = HybridSmem<T>::bytes(2, p.G, p.n, p.scratch_rows, false, p.ct, Log2<K>::value);
+  if (smem > (size_t)dev.max_smem_optin) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, p.ct, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  long grid = (long)per_sm * dev.sm_count;
+  if (grid > p.ntiles) grid = p.ntiles;
+  kern<<<(unsigned)grid, p.ct, smem, stream>>>(p);
+  return cudaGetLastError();
+}
+
 template <class T, int K, bool WARP, int LSTRIDE>
 cudaError_t launch_one(const HybridParams& p0, const DeviceInfo& dev, cudaStream_t stream) {
   constexpr int MAXT = WARP ? kWarpThreads : kBlockThreads;
@@ -80,6 +100,10 @@ cudaError_t launch_one(const HybridParams& p0, const DeviceInfo& dev, cudaStream
   // shapes and PCR on 16 rows per thread would spill)
   if constexpr (WARP && sizeof(T) == 4 && !(K == 16 && LSTRIDE == 1)) {
     if (tma_ok && tunable(TRIDI_TUNE_WARP_STREAMS) != 2) return launch_warp_streams<T, K, LSTRIDE>(p, dev, stream);
+  }
+  if constexpr (!WARP && sizeof(T) == 4 && !(K == 16 && LSTRIDE == 1)) {
+    if (tma_ok && p.ct == 128 && tunable(TRIDI_TUNE_WARP_STREAMS) != 2)
+      return launch_block_streams<T, K, LSTRIDE>(p, dev, stream);
   }
   const int logk = Log2<K>::value;
   const size_t stage_bytes = HybridSmem<T>::stage_elems(p.G, p.n) * sizeof(T);

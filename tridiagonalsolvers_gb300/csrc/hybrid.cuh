@@ -541,4 +541,76 @@ __global__ void __launch_bounds__(kWarpKernelThreads, MINB) hybrid_warp_kernel(H
   }
 }
 
+// Block shapes (a system's group spans several warps) without a producer
+// warp: the CTA is one or more groups (ct = max(tps, 128) threads), every
+// thread solves, and thread 0 streams the CTA's tiles through a two-buffer
+// ring: tiles k and k+1 are in flight while tile k is read into registers;
+// after a CTA barrier (everyone has read buffer s) tile k+2 is issued into
+// it, then the solve runs.  Same arithmetic as hybrid_kernel.
+template <class T, int K, int LSTRIDE, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) hybrid_block_stream_kernel(HybridParams p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  const int n = p.n, G = p.G, tps = p.tps, ct = p.ct;
+  T* stages = reinterpret_cast<T*>(smem + HybridSmem<T>::barrier_bytes());
+  const size_t stage_elems = HybridSmem<T>::stage_elems(G, n);
+  const int tid = threadIdx.x;
+  const T* ga = static_cast<const T*>(p.a);
+  const T* gb = static_cast<const T*>(p.b);
+  const T* gc = static_cast<const T*>(p.c);
+  const T* gd = static_cast<const T*>(p.d);
+  T* gx = static_cast<T*>(p.x);
+  const auto issue = [&](int tile, int s) {  // thread 0
+    const long sys0 = (long)tile * G;
+    const long nsys = (p.m - sys0) < G ? (p.m - sys0) : G;
+    const uint32_t bytes = (uint32_t)(nsys * n * sizeof(T));
+    T* st = stages + s * stage_elems;
+    mbar_arrive_expect_tx(&bars[s], 4 * bytes);
+    bulk_g2s(st + 0 * (size_t)G * n, ga + sys0 * n, bytes, &bars[s]);
+    bulk_g2s(st + 1 * (size_t)G * n, gb + sys0 * n, bytes, &bars[s]);
+    bulk_g2s(st + 2 * (size_t)G * n, gc + sys0 * n, bytes, &bars[s]);
+    bulk_g2s(st + 3 * (size_t)G * n, gd + sys0 * n, bytes, &bars[s]);
+  };
+  if (tid == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_fence_init();
+    if ((int)blockIdx.x < p.ntiles) issue(blockIdx.x, 0);
+    if ((int)(blockIdx.x + gridDim.x) < p.ntiles) issue(blockIdx.x + gridDim.x, 1);
+  }
+  __syncthreads();
+
+  const int g = tid / tps;
+  const int t = tid - g * tps;
+  T* base = stages + 2 * stage_elems;
+  const size_t rows = p.scratch_rows;
+  T* mine = base + (size_t)g * 5 * rows;
+  const GroupScratch<T> sc{mine, mine + rows, mine + 2 * rows, mine + 3 * rows, mine + 4 * rows};
+  Row<T>* exports = reinterpret_cast<Row<T>*>(base + (size_t)G * 5 * rows);
+  int k = 0;
+  for (int tile = blockIdx.x; tile < p.ntiles; tile += gridDim.x, ++k) {
+    const int s = k & 1;
+    const bool ok = consumer_sync_and(ct, mbar_wait(&bars[s], (k >> 1) & 1, p.status));
+    if (!ok) break;
+    const T* st = stages + s * stage_elems + (size_t)g * n + (size_t)t * K;
+    T va[K], vb[K], vc[K], vd[K];
+    load_vec_smem<T, K>(st + 0 * (size_t)G * n, va);
+    load_vec_smem<T, K>(st + 1 * (size_t)G * n, vb);
+    load_vec_smem<T, K>(st + 2 * (size_t)G * n, vc);
+    load_vec_smem<T, K>(st + 3 * (size_t)G * n, vd);
+    consumer_sync(ct);  // buffer s read by every thread
+    if (tid == 0 && tile + 2 * (int)gridDim.x < p.ntiles) {
+      fence_proxy_async_smem();
+      issue(tile + 2 * gridDim.x, s);
+    }
+    Row<T> r[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) r[i] = Row<T>{va[i], vb[i], vc[i], vd[i]};
+    T xr[K];
+    hybrid_solve<T, K, false, LSTRIDE>(r, xr, t, tps, p.stride, sc, exports, ct);
+    const long sys = (long)tile * G + g;
+    if (sys < p.m) store_vec<T, K>(gx + sys * n + (long)t * K, xr);
+  }
+}
+
 }  // namespace tridi
