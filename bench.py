@@ -55,6 +55,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def rel_residual64(a, b, c, d, x):
+    """Per system ||d - T x||_2 / ||d||_2 in FP64, rows are systems (a[:, 0]
+    and c[:, -1] ignored): the guard that a timed result solves its systems."""
+    a, b, c, d, x = (np.asarray(v, np.float64) for v in (a, b, c, d, x))
+    r = d - b * x
+    r[:, 1:] -= a[:, 1:] * x[:, :-1]
+    r[:, :-1] -= c[:, :-1] * x[:, 1:]
+    return np.linalg.norm(r, axis=1) / np.maximum(np.linalg.norm(d, axis=1), 1e-300)
+
+
 def profile_value(name: str, key: str):
     """A figure recorded in a committed ncu summary under profiles/ (None if absent)."""
     p = ROOT / "profiles" / name
@@ -240,12 +250,10 @@ def run_gpu(args):
     step()
     torch.cuda.synchronize()
     if rank == 0:
-        from oracle import gold
-
         xs = tx[:32].cpu().numpy()
-        res = gold.rel_residual(a[:32], b[:32], c[:32], d[:32], xs).max()
+        res = rel_residual64(a[:32], b[:32], c[:32], d[:32], xs).max()
         if not res < 2e-6:
-            raise SystemExit(f"bench: cr result fails the oracle check (residual {res:.2e})")
+            raise SystemExit(f"bench: cr result fails the residual check (residual {res:.2e})")
 
     for _ in range(args.warmup):
         step()
@@ -286,11 +294,9 @@ def run_gpu(args):
     barrier(world)
     e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world, dev)
     if rank == 0:
-        from oracle import gold
-
-        res = gold.rel_residual(a[:32], b[:32], c[:32], d[:32], hx[:32].numpy()).max()
+        res = rel_residual64(a[:32], b[:32], c[:32], d[:32], hx[:32].numpy()).max()
         if not res < 2e-6:
-            raise SystemExit(f"bench: drop-in cr result fails the oracle check (residual {res:.2e})")
+            raise SystemExit(f"bench: drop-in cr result fails the residual check (residual {res:.2e})")
 
     # ---- per-kernel table on the same batch (outside the timed region) ----
     peak, peak_kind = measured_peaks()
