@@ -80,6 +80,8 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
 #define TRIDI_TUNE_NBC_KERNEL 8   /* bank-conflict-free CR: 0/1 = the register kernel where it has the shape
                                      (same arithmetic and results, about twice as fast), 2 = the
                                      shared-memory kernel always */
+#define TRIDI_TUNE_DROPIN_CHUNK 9 /* host-pointer launchers: KiB of each coefficient array per pipelined chunk
+                                     (0 = 8192) */
 tridi_status tridi_set_tunable(int key, int value);
 int tridi_get_tunable(int key);
 

@@ -73,16 +73,20 @@ tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d
   std::lock_guard<std::mutex> lock(g_mu);
   Workspace& w = g_ws[dev];
 
-  // Chunks of about 32 MiB of input (8 MiB per coefficient array), whole
-  // systems, at most 16 chunks.
+  // Chunks of about 32 MiB of input (8 MiB per coefficient array, or
+  // TRIDI_TUNE_DROPIN_CHUNK KiB), whole systems, at most 64 chunks.
   const size_t sys_bytes = (size_t)n * sizeof(T);
-  long per = (long)((8u << 20) / sys_bytes);
+  const int chunk_kib = tunable(TRIDI_TUNE_DROPIN_CHUNK);
+  const size_t chunk_bytes = chunk_kib > 0 ? (size_t)chunk_kib << 10 : (size_t)8 << 20;
+  long per = (long)(chunk_bytes / sys_bytes);
   if (per < 1) per = 1;
-  if (per * 16 < m) per = (m + 15) / 16;
+  if (per * 64 < m) per = (m + 63) / 64;
   if (per > m) per = m;
   const size_t arr = align256((size_t)m * sys_bytes);
-  const size_t scratch = align256(algo_scratch<T>(algo, n, m, param));
-  if ((e = ensure_workspace(w, 5 * arr + scratch)) != cudaSuccess) return cuda_status(e);
+  // chunks use disjoint slices of the scratch, each sized for a full chunk
+  const long nchunks = (m + per - 1) / per;
+  const size_t ws_share = align256(algo_scratch<T>(algo, n, (int)per, param));
+  if ((e = ensure_workspace(w, 5 * arr + (size_t)nchunks * ws_share)) != cudaSuccess) return cuda_status(e);
   char* base = static_cast<char*>(w.ptr);
   T* da = reinterpret_cast<T*>(base);
   T* db = reinterpret_cast<T*>(base + arr);
@@ -103,11 +107,8 @@ tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d
       st = cuda_status(e);
       break;
     }
-    // Chunks use disjoint slices of the scratch: give each its share.
-    const size_t ws_share = scratch / ((m + per - 1) / per);
     st = dropin_device_solve<T>(algo, da + off, db + off, dc + off, dd + off, dx + off, n, (int)cnt, param,
-                                static_cast<char*>(ws) + (size_t)k * (ws_share & ~size_t(255)),
-                                ws_share & ~size_t(255), s);
+                                static_cast<char*>(ws) + (size_t)k * ws_share, ws_share, s);
     if (st != TRIDI_SUCCESS) break;
     if ((e = cudaMemcpyAsync(x + off, dx + off, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
       st = cuda_status(e);
