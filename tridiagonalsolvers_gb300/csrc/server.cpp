@@ -7,7 +7,7 @@
 //     into one ragged batch (up to max_batch_rows rows), and hands the batch
 //     to that slot;
 //   * each slot's worker runs its batch on the slot's own stream:
-//     stream-ordered cudaMallocAsync, host -> device transfer straight from the
+//     stream-ordered allocation from the server's pool, host -> device transfer straight from the
 //     callers' arrays, an asynchronous plan upload, the fused refinement
 //     (FP32 solves, extended-precision residual and accumulation, `sweeps`
 //     corrections), the batch's maximum residual read back, one more sweep
@@ -220,6 +220,18 @@ class Server {
     cudaError_t e;
     if ((e = cudaGetDevice(&device_)) != cudaSuccess) return cuda_status(e);
     if (tridi_init() != TRIDI_SUCCESS) return TRIDI_ERROR_CUDA;
+    // The server's own stream-ordered pool, keeping up to the budget mapped
+    // between batches: the default pool returns its memory at every
+    // synchronisation, and re-mapping it per batch cost more than the
+    // transfers on some hosts.
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device_;
+    if ((e = cudaMemPoolCreate(&mempool_, &props)) != cudaSuccess) return cuda_status(e);
+    unsigned long long keep = budget_;
+    if ((e = cudaMemPoolSetAttribute(mempool_, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess)
+      return cuda_status(e);
     for (auto* s : slots_) {
       s->server = this;
       if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -273,6 +285,7 @@ class Server {
       if (s->stream) cudaStreamDestroy(s->stream);
       delete s;
     }
+    if (mempool_) cudaMemPoolDestroy(mempool_);
     for (auto& kv : all_) delete kv.second;
   }
 
@@ -469,7 +482,7 @@ class Server {
     size_t total = 0;
     for (size_t v : sizes) total += v;
     char* dmem = nullptr;
-    if ((e = cudaMallocAsync(reinterpret_cast<void**>(&dmem), total, st)) != cudaSuccess) {
+    if ((e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&dmem), total, mempool_, st)) != cudaSuccess) {
       tridi_ragged_plan_destroy(plan);
       return cuda_status(e);
     }
@@ -653,6 +666,7 @@ class Server {
   long max_rows_;
   int sweeps_, max_sweeps_;
   int device_ = 0;
+  cudaMemPool_t mempool_ = nullptr;
   std::vector<Slot*> slots_;
   std::mutex mu_;
   std::condition_variable cv_, done_cv_;
