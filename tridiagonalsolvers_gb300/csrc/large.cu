@@ -31,7 +31,8 @@ tridi_status partition_solve_device(const T* a, const T* b, const T* c, const T*
                                     tridi_stream_t stream);
 bool large_tma_ok(const float* a, const float* b, const float* c, const float* d, long n, long m);
 tridi_status large_tma_pass(bool back, const float* a, const float* b, const float* c, const float* d, long n,
-                            long m, long P, long PMp, float* iface, const float* sol, float* x, cudaStream_t st);
+                            long m, long P, long PMp, float* red, float* bnd, const float* sol, float* x,
+                            cudaStream_t st);
 
 struct LargeParams {
   const void* a;
@@ -216,14 +217,17 @@ tridi_status large_solve_device(const T* a, const T* b, const T* c, const T* d, 
   bool tma = false;
   if constexpr (sizeof(T) == 4) tma = layout == 1 && tunable(TRIDI_TUNE_LARGE_TMA) != 2 && large_tma_ok(a, b, c, d, n, m);
   if (tma) {
+    // the separator rows assembled in the pass (the interface area holds the
+    // tile-boundary arrays only)
     const tridi_status t = large_tma_pass(false, reinterpret_cast<const float*>(a), reinterpret_cast<const float*>(b),
                                           reinterpret_cast<const float*>(c), reinterpret_cast<const float*>(d), n, m,
-                                          p.P, p.PMp, static_cast<float*>(p.iface), nullptr, nullptr, st);
+                                          p.P, p.PMp, static_cast<float*>(p.red), static_cast<float*>(p.iface),
+                                          nullptr, nullptr, st);
     if (t != TRIDI_SUCCESS) return t;
   } else {
     large_reduce_kernel<T, kChunk><<<blocks, 256, 0, st>>>(p);
+    large_assemble_kernel<T><<<blocks, 256, 0, st>>>(p);
   }
-  large_assemble_kernel<T><<<blocks, 256, 0, st>>>(p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e);
   const T* r = static_cast<const T*>(p.red);
@@ -238,7 +242,7 @@ tridi_status large_solve_device(const T* a, const T* b, const T* c, const T* d, 
   if (tma)
     return large_tma_pass(true, reinterpret_cast<const float*>(a), reinterpret_cast<const float*>(b),
                           reinterpret_cast<const float*>(c), reinterpret_cast<const float*>(d), n, m, p.P, p.PMp,
-                          nullptr, static_cast<const float*>(p.sol), reinterpret_cast<float*>(x), st);
+                          nullptr, nullptr, static_cast<const float*>(p.sol), reinterpret_cast<float*>(x), st);
   large_back_kernel<T, kChunk><<<blocks, 256, 0, st>>>(p);
   return cuda_status(cudaGetLastError());
 }

@@ -41,12 +41,28 @@ constexpr size_t kLtSmem = 128 + (size_t)kStages * 4 * kTileFloats * sizeof(floa
 
 struct LtParams {
   long n, m, P, PMp;
-  float* iface;     // reduce: 10 arrays of P*m (stride PMp)
+  float* red;       // reduce: the separator system, 4 arrays of P*m (stride PMp)
+  float* bnd;       // reduce: tile-boundary interface, 10 arrays of row_tiles*m (stride BS)
+  long BS;
   const float* sol; // back: separators
   float* x;         // back: solution
   int row_tiles, col_tiles;
   unsigned* status;
 };
+constexpr int kBndLast = 0;   // bnd arrays 0..6: lD, lC, lA and the separator row of a tile's last chunk
+constexpr int kBndFirst = 7;  // bnd arrays 7..9: fD, fC, fA of a tile's first chunk
+constexpr size_t kLtExchange = 2 * kLtWarps * 32 * 3 * sizeof(float);  // reduce: fD, fC, fA per lane, two tiles
+
+// Separator row of a chunk (partition.cuh's separator_row_s) from its
+// summary and the next chunk's first-row coefficients, into the 4 arrays
+// of the separator system at index o.
+__device__ __forceinline__ void put_separator(float* red, long S, long o, const Row<float>& sep, float lD, float lC,
+                                              float lA, float nD, float nC, float nA) {
+  red[0 * S + o] = -sep.a * lA;
+  red[1 * S + o] = sep.b - sep.a * lC - sep.c * nA;
+  red[2 * S + o] = -sep.c * nC;
+  red[3 * S + o] = sep.d - sep.a * lD - sep.c * nD;
+}
 
 __device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
   asm volatile(
@@ -139,10 +155,14 @@ __global__ void __launch_bounds__(32 * (kLtWarps + 1), 1)
   }
 
   // ---------------- consumers ----------------
+  // (the reduce pass exchanges first-row coefficients between its warps
+  // through shared memory, so the consumers agree on every wait's outcome
+  // and leave together)
+  float* exch = reinterpret_cast<float*>(smem + kLtSmem);
   int k = 0;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
     const int s = k % kStages;
-    if (!mbar_wait(&full[s], (k / kStages) & 1, p.status)) return;
+    if (!named_sync_and(1, 32 * kLtWarps, mbar_wait(&full[s], (k / kStages) & 1, p.status))) return;
     const long sys = (long)(t % p.col_tiles) * kTileCols + lane;
     const long r0 = (long)(t / p.col_tiles) * kTileRows + (long)warp * kLtChunk;  // the lane's first row
     const long j = r0 / kLtChunk;                                                 // its chunk
@@ -153,6 +173,7 @@ __global__ void __launch_bounds__(32 * (kLtWarps + 1), 1)
     float* sd = st + 3 * kTileFloats;
     const long rem = p.n - r0;
     const int kr = rem <= 0 ? 0 : (rem < kLtChunk ? (int)rem : kLtChunk);
+    ChunkSummary<float> cs;
     if (kr > 0) {
       const long o = j * p.m + sys;
       float sj = 0.f, sl = 0.f;
@@ -160,15 +181,8 @@ __global__ void __launch_bounds__(32 * (kLtWarps + 1), 1)
         sj = p.sol[o];
         sl = j > 0 ? p.sol[o - p.m] : 0.f;
       }
-      ChunkSummary<float> cs;
       column_eliminate(cs, kr, j == 0, j == p.P - 1, sa, sb, sc, sd);
-      if constexpr (!BACK) {
-        float* f = p.iface;
-        const long S = p.PMp;
-        f[0 * S + o] = cs.fD; f[1 * S + o] = cs.fC; f[2 * S + o] = cs.fA;
-        f[3 * S + o] = cs.lD; f[4 * S + o] = cs.lC; f[5 * S + o] = cs.lA;
-        f[6 * S + o] = cs.sep.a; f[7 * S + o] = cs.sep.b; f[8 * S + o] = cs.sep.c; f[9 * S + o] = cs.sep.d;
-      } else {
+      if constexpr (BACK) {
         float* gx = p.x + r0 * p.m + sys;
         gx[(long)(kr - 1) * p.m] = sj;
         float xn = sj;
@@ -182,8 +196,55 @@ __global__ void __launch_bounds__(32 * (kLtWarps + 1), 1)
         }
       }
     }
+    if constexpr (!BACK) {
+      // separator rows: warp w < 7 takes the next chunk's first row from warp
+      // w + 1 of the same tile; a tile's last chunk and its first chunk go to
+      // the boundary arrays, assembled by large_tile_boundary_kernel
+      float* ex = exch + (k & 1) * (kLtWarps * 32 * 3);
+      float* mine = ex + (warp * 32 + lane) * 3;
+      mine[0] = kr > 0 ? cs.fD : 0.f;
+      mine[1] = kr > 0 ? cs.fC : 0.f;
+      mine[2] = kr > 0 ? cs.fA : 0.f;
+      consumer_sync(32 * kLtWarps);
+      if (kr > 0) {
+        const long tr = t / p.col_tiles;
+        if (warp + 1 < kLtWarps) {
+          const float* nx = ex + ((warp + 1) * 32 + lane) * 3;
+          put_separator(p.red, p.PMp, j * p.m + sys, cs.sep, cs.lD, cs.lC, cs.lA, nx[0], nx[1], nx[2]);
+        } else {
+          float* b = p.bnd + tr * p.m + sys;
+          b[(kBndLast + 0) * p.BS] = cs.lD; b[(kBndLast + 1) * p.BS] = cs.lC; b[(kBndLast + 2) * p.BS] = cs.lA;
+          b[(kBndLast + 3) * p.BS] = cs.sep.a; b[(kBndLast + 4) * p.BS] = cs.sep.b;
+          b[(kBndLast + 5) * p.BS] = cs.sep.c; b[(kBndLast + 6) * p.BS] = cs.sep.d;
+        }
+        if (warp == 0) {
+          float* b = p.bnd + tr * p.m + sys;
+          b[(kBndFirst + 0) * p.BS] = cs.fD; b[(kBndFirst + 1) * p.BS] = cs.fC; b[(kBndFirst + 2) * p.BS] = cs.fA;
+        }
+      }
+    }
     release_stage(&empty[s]);
   }
+}
+
+// Separator rows of the tiles' last chunks (chunk 8 tr + 7 of every tile row
+// tr), whose next chunk opens the next tile row: one thread per (tr, system).
+__global__ void __launch_bounds__(256) large_tile_boundary_kernel(LtParams p) {
+  const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (long)p.row_tiles * p.m) return;
+  const long tr = gid / p.m, sys = gid - tr * p.m;
+  const long j = tr * kLtWarps + kLtWarps - 1;
+  if (j >= p.P) return;  // the system's last chunk lies in an earlier warp of this tile
+  const float* b = p.bnd + gid;
+  const Row<float> sep{b[(kBndLast + 3) * p.BS], b[(kBndLast + 4) * p.BS], b[(kBndLast + 5) * p.BS],
+                       b[(kBndLast + 6) * p.BS]};
+  float nD = 0.f, nC = 0.f, nA = 0.f;
+  if (j + 1 < p.P) {
+    const float* f = b + p.m;  // tile row tr + 1, the same system
+    nD = f[(kBndFirst + 0) * p.BS]; nC = f[(kBndFirst + 1) * p.BS]; nA = f[(kBndFirst + 2) * p.BS];
+  }
+  put_separator(p.red, p.PMp, j * p.m + sys, sep, b[(kBndLast + 0) * p.BS], b[(kBndLast + 1) * p.BS],
+                b[(kBndLast + 2) * p.BS], nD, nC, nA);
 }
 
 // The driver's tensor-map encoder, looked up through the runtime once (the
@@ -224,17 +285,26 @@ bool large_tma_ok(const float* a, const float* b, const float* c, const float* d
          n < (1L << 31) && m < (1L << 31);
 }
 
-// One TMA pass: back = false -> interface (reduce), true -> x (back).
+// Bytes of the boundary arrays of a reduce pass (within the 10 * PMp
+// interface floats the register kernels use).
+long large_tma_boundary_stride(long n, long m) { return ((((n + kTileRows - 1) / kTileRows) * m) + 63) & ~63L; }
+
+// One TMA pass: back = false -> the separator system (reduce, with the
+// assembly of separator rows fused in; bnd: scratch of 10 boundary arrays),
+// true -> x (back).
 tridi_status large_tma_pass(bool back, const float* a, const float* b, const float* c, const float* d, long n,
-                            long m, long P, long PMp, float* iface, const float* sol, float* x, cudaStream_t st) {
+                            long m, long P, long PMp, float* red, float* bnd, const float* sol, float* x,
+                            cudaStream_t st) {
   const DeviceInfo* dev = current_device();
   if (!dev) return TRIDI_ERROR_CUDA;
-  if ((size_t)dev->max_smem_optin < kLtSmem) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  const size_t smem = back ? kLtSmem : kLtSmem + kLtExchange;
+  if ((size_t)dev->max_smem_optin < smem) return TRIDI_ERROR_UNSUPPORTED_SIZE;
   CUtensorMap ma, mb, mc, md;
   if (!make_map(&ma, a, n, m) || !make_map(&mb, b, n, m) || !make_map(&mc, c, n, m) || !make_map(&md, d, n, m))
     return TRIDI_ERROR_INVALID_VALUE;
   LtParams p{};
-  p.n = n; p.m = m; p.P = P; p.PMp = PMp; p.iface = iface; p.sol = sol; p.x = x;
+  p.n = n; p.m = m; p.P = P; p.PMp = PMp; p.red = red; p.bnd = bnd; p.sol = sol; p.x = x;
+  p.BS = large_tma_boundary_stride(n, m);
   p.row_tiles = (int)((n + kTileRows - 1) / kTileRows);
   p.col_tiles = (int)(m / kTileCols);
   p.status = dev->status;
@@ -249,9 +319,12 @@ tridi_status large_tma_pass(bool back, const float* a, const float* b, const flo
     large_tile_kernel<true><<<grid, 32 * (kLtWarps + 1), kLtSmem, st>>>(p, ma, mb, mc, md);
   } else {
     if ((e = cudaFuncSetAttribute(large_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kLtSmem)) != cudaSuccess)
+                                  (int)smem)) != cudaSuccess)
       return cuda_status(e);
-    large_tile_kernel<false><<<grid, 32 * (kLtWarps + 1), kLtSmem, st>>>(p, ma, mb, mc, md);
+    large_tile_kernel<false><<<grid, 32 * (kLtWarps + 1), smem, st>>>(p, ma, mb, mc, md);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+    const long cnt = (long)p.row_tiles * m;
+    large_tile_boundary_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, st>>>(p);
   }
   return cuda_status(cudaGetLastError());
 }
