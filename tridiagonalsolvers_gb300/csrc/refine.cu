@@ -286,6 +286,9 @@ tridi_status refine_device(const float* a, const float* b, const float* c, const
   RefineParams p{};
   p.a = a; p.b = b; p.c = c; p.d = d; p.e = w.e; p.r = w.r; p.rr = w.rr; p.dd = w.dd;
   p.n = n; p.m = m; p.layout = layout;
+  // x_k alternates between the workspace copy and x; the first update
+  // writes the workspace, so one correction (the usual case) ends in x and
+  // the FP64 mode needs no final copy
   double* bufs[2] = {x, w.xalt};
   int cur = 0;  // x_k lives in bufs[cur]
   double rel = 0.0;
@@ -294,7 +297,6 @@ tridi_status refine_device(const float* a, const float* b, const float* c, const
     p.first = sweep == 0;
     p.xin = bufs[cur];
     p.xout = bufs[cur ^ 1];
-    if (sweep == 0) p.xout = x;  // the first update writes x directly
     if ((e = cudaMemsetAsync(w.rr, 0, sizeof(double) * m, st)) != cudaSuccess) return cuda_status(e);
     unsigned blocks;
     if (layout == 0) {
