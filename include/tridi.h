@@ -186,6 +186,11 @@ tridi_status tridi_solve_large_f64(const double *a, const double *b, const doubl
      TRIDI_AUTOTUNE_CR_ROWS           key n (power of two, 32..4096): rows per
         thread (4, 8 or 16; threads per system = n / rows) of the FP32
         cr / pcr / crpcr kernels; diagonally dominant systems, timed on cr.
+     TRIDI_AUTOTUNE_RAGGED_REFINE_THREADS  as TRIDI_AUTOTUNE_RAGGED_THREADS,
+        timed on the fused one-correction refinement instead of the plain
+        solve, for plans created afterwards by tridi_ragged_plan_create_refine
+        (the refinement issues ~3x the instructions per row of the plain
+        solve, so its best group width per size can differ).
    tridi_tuned / tridi_set_tuned read and write the table (key as above,
    0 = not tuned: the built-in choice applies), tridi_autotune_reset clears
    it.  Synchronises `stream`; allocates and frees its own sample. */
@@ -193,6 +198,7 @@ tridi_status tridi_solve_large_f64(const double *a, const double *b, const doubl
 #define TRIDI_AUTOTUNE_PCR_THOMAS_SPLIT 1
 #define TRIDI_AUTOTUNE_RAGGED_THREADS 2
 #define TRIDI_AUTOTUNE_CR_ROWS 3
+#define TRIDI_AUTOTUNE_RAGGED_REFINE_THREADS 4
 tridi_status tridi_autotune(int table, long key, long sample_unknowns, tridi_stream_t stream, int *chosen,
                             float *best_ms);
 int tridi_tuned(int table, long key);
@@ -208,6 +214,10 @@ tridi_status tridi_autotune_reset(void);
    a, b, c, d, x: device, 16-byte aligned, at least round_up(total_rows, 4)
    elements each. */
 tridi_status tridi_ragged_plan_create(const long *offsets, int num_systems, void **plan);
+/* The same for a batch that will be refined (tridi_ragged_refine_f32): threads
+   per system from the TRIDI_AUTOTUNE_RAGGED_REFINE_THREADS table where tuned,
+   else as tridi_ragged_plan_create.  Either kind of plan serves both calls. */
+tridi_status tridi_ragged_plan_create_refine(const long *offsets, int num_systems, void **plan);
 size_t tridi_ragged_plan_device_bytes(const void *plan);
 int tridi_ragged_plan_items(const void *plan);
 long tridi_ragged_plan_total_rows(const void *plan);

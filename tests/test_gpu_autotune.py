@@ -94,3 +94,40 @@ def test_tune_cr_rows_then_solve(cuda, n):
         autotune.set_table({"cr_rows": {str(n): rr}})
         x = tg.cr(*t).cpu().numpy()
         assert gold.rel_residual(a, b, c, d, x).max() <= RES_TOL[np.float32], rr
+
+
+def test_tune_ragged_refine_buckets_and_refine(cuda):
+    """The refinement's own table: tuned on the fused refinement, read only by
+    refinement plans (plain plans keep the plain table), and every forced
+    choice refines every system to 1e-10."""
+    import torch
+
+    from tridiagonalsolvers_gb300.ragged import RaggedRefiner
+
+    for k in (256, 4096):
+        th, ms = autotune.tune("ragged_refine", k, sample_unknowns=1 << 22)
+        assert th in (32, 160, 480) and ms > 0
+        assert autotune.table()["ragged_refine"][str(k)] == th
+    sizes = np.array([40, 100, 700, 1500, 3000, 5000, 8000, 300, 64])
+    a, b, c, d, off = workloads.adi(sizes, seed=6)
+    total = int(off[-1])
+
+    def dev(v):
+        t = torch.zeros(padded(total), dtype=torch.float32, device=cuda)
+        t[:total] = torch.from_numpy(v)
+        return t
+
+    t = [dev(v) for v in (a, b, c, d)]
+    autotune.set_table({"ragged": {str(1 << k): 32 for k in range(5, 15)}})
+    plain_items = RaggedPlan(off).items
+    for th in (32, 160, 480):
+        autotune.set_table({"ragged_refine": {str(1 << k): th for k in range(5, 15)}})
+        assert RaggedPlan(off).items == plain_items  # plain plans ignore the refinement's table
+        plan = RaggedPlan(off, refine=True)
+        x, rel = RaggedRefiner(plan, *t, sweeps=1, graph=False).run()
+        x = x.cpu().numpy()[:total]
+        assert rel <= 1e-10, th
+        for s in range(len(sizes)):
+            lo, hi = off[s], off[s + 1]
+            sl = [v[lo:hi][None] for v in (a, b, c, d)]
+            assert gold.rel_residual(*sl, x[lo:hi][None])[0] <= 1e-10, (th, s)

@@ -54,6 +54,7 @@ _SIGS["tridi_write_result_file_f32"] = (c_int, [_P, c_int, c_int, c_char_p])
 _SIGS["tridi_write_result_file_f64"] = (c_int, [_P, c_int, c_int, c_char_p])
 _SIGS["tridi_large_workspace_bytes"] = (c_size_t, [ctypes.c_long, ctypes.c_long, c_int])
 _SIGS["tridi_ragged_plan_create"] = (c_int, [_P, c_int, POINTER(c_void_p)])
+_SIGS["tridi_ragged_plan_create_refine"] = (c_int, [_P, c_int, POINTER(c_void_p)])
 _SIGS["tridi_ragged_plan_device_bytes"] = (c_size_t, [_P])
 _SIGS["tridi_ragged_plan_items"] = (c_int, [_P])
 _SIGS["tridi_ragged_plan_upload"] = (c_int, [_P, _P, c_size_t, _P])

@@ -9,7 +9,10 @@ in csrc/autotune.cu).  Tunes, on the GPU in use:
                      [2^k, 2^(k+1)) of the ragged work queue, used by plans
                      created afterwards;
   * cr_rows       -- rows per thread (4, 8, 16) of the FP32 CR / PCR / CR-PCR
-                     kernels per power-of-two n (threads per system = n / rows).
+                     kernels per power-of-two n (threads per system = n / rows);
+  * ragged_refine -- as `ragged`, timed on the fused one-correction refinement,
+                     used by plans created afterwards with RaggedPlan(...,
+                     refine=True) and by the solve server.
 
     from tridiagonalsolvers_gb300 import autotune
     table = autotune.tune_all()            # {"ragged": {"32": 32, ...}, ...}
@@ -22,12 +25,13 @@ import json
 
 from ._lib import check, lib
 
-TABLES = {"crpcr_rest": 0, "pcr_thomas": 1, "ragged": 2, "cr_rows": 3}
+TABLES = {"crpcr_rest": 0, "pcr_thomas": 1, "ragged": 2, "cr_rows": 3, "ragged_refine": 4}
 DEFAULT_KEYS = {
     "crpcr_rest": [1 << k for k in range(2, 13)],
     "pcr_thomas": [1 << k for k in range(1, 13)],
     "ragged": [1 << k for k in range(5, 15)],  # buckets [32, 64) .. [16384, 32768)
     "cr_rows": [1 << k for k in range(5, 13)],
+    "ragged_refine": [1 << k for k in range(5, 15)],
 }
 
 
@@ -43,7 +47,8 @@ def tune(table: str, key: int, sample_unknowns: int = 1 << 24, stream=None) -> t
     return chosen.value, ms.value
 
 
-def tune_all(tables=("ragged", "crpcr_rest", "pcr_thomas", "cr_rows"), sample_unknowns: int = 1 << 24) -> dict:
+def tune_all(tables=("ragged", "crpcr_rest", "pcr_thomas", "cr_rows", "ragged_refine"),
+             sample_unknowns: int = 1 << 24) -> dict:
     out = {}
     for t in tables:
         out[t] = {str(k): tune(t, k, sample_unknowns)[0] for k in DEFAULT_KEYS[t]}

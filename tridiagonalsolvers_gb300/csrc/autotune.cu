@@ -10,6 +10,9 @@
 //                                    ragged work queue (32, 160 or 480)
 //   TRIDI_AUTOTUNE_CR_ROWS           rows per thread of the FP32 CR / PCR /
 //                                    CR-PCR kernels per power-of-two n
+//   TRIDI_AUTOTUNE_RAGGED_REFINE_THREADS  threads per system per size bucket
+//                                    of plans for the fused refinement, timed
+//                                    on that refinement (one correction)
 //
 // The choices land in the process-wide table of runtime.cu (tridi_tuned /
 // tridi_set_tuned); the Python layer saves and reloads it as JSON.
@@ -165,7 +168,8 @@ extern "C" tridi_status tridi_autotune(int table, long key, long sample, tridi_s
     }
     tridi_set_tuned(table, key, saved);
     if (ts != TRIDI_SUCCESS && ts != TRIDI_ERROR_UNSUPPORTED_SIZE) return ts;
-  } else if (table == TRIDI_AUTOTUNE_RAGGED_THREADS) {
+  } else if (table == TRIDI_AUTOTUNE_RAGGED_THREADS || table == TRIDI_AUTOTUNE_RAGGED_REFINE_THREADS) {
+    const bool refine = table == TRIDI_AUTOTUNE_RAGGED_REFINE_THREADS;
     const int k = ilog2(key);
     const long lo = 1L << k;
     long hi = (2L << k) - 1;
@@ -179,11 +183,22 @@ extern "C" tridi_status tridi_autotune(int table, long key, long sample, tridi_s
     Sample smp;
     tridi_status ts = smp.alloc(off.back() + 4, st, 1);
     if (ts != TRIDI_SUCCESS) return ts;
+    // the refinement's FP64 solution, workspace and residual word
+    const size_t wsb = refine ? tridi_ragged_refine_workspace_bytes(off.back(), nsys) : 0;
+    void* rbuf = nullptr;
+    if (refine) {
+      const cudaError_t e = cudaMalloc(&rbuf, wsb + sizeof(double) * (size_t)(off.back() + 4 + 31 + 32));
+      if (e != cudaSuccess) return cuda_status(e);
+    }
+    double* x64 = static_cast<double*>(rbuf);
+    double* rel = x64 + ((off.back() + 4 + 31) & ~31L);
+    void* ws = rel + 32;
     const int saved = tuned(table, k);
     for (int th : {32, 160, 480}) {
       tridi_set_tuned(table, key, th);
       void* plan = nullptr;
-      ts = tridi_ragged_plan_create(off.data(), nsys, &plan);
+      ts = refine ? tridi_ragged_plan_create_refine(off.data(), nsys, &plan)
+                  : tridi_ragged_plan_create(off.data(), nsys, &plan);
       if (ts != TRIDI_SUCCESS) break;
       const size_t pb = tridi_ragged_plan_device_bytes(plan);
       void* dp = nullptr;
@@ -196,8 +211,13 @@ extern "C" tridi_status tridi_autotune(int table, long key, long sample, tridi_s
       ts = tridi_ragged_plan_upload(plan, dp, pb, stream);
       float ms = 0.f;
       if (ts == TRIDI_SUCCESS)
-        ts = time_ms([&]() { return tridi_ragged_solve_f32(smp.a, smp.b, smp.c, smp.d, smp.x, plan, dp, stream); },
-                     st, &ms);
+        ts = time_ms(
+            [&]() {
+              return refine ? tridi_ragged_refine_f32(smp.a, smp.b, smp.c, smp.d, x64, plan, dp, nullptr, 1, ws, wsb,
+                                                      rel, stream)
+                            : tridi_ragged_solve_f32(smp.a, smp.b, smp.c, smp.d, smp.x, plan, dp, stream);
+            },
+            st, &ms);
       cudaFree(dp);
       tridi_ragged_plan_destroy(plan);
       if (ts != TRIDI_SUCCESS) break;
@@ -207,6 +227,7 @@ extern "C" tridi_status tridi_autotune(int table, long key, long sample, tridi_s
       }
     }
     tridi_set_tuned(table, key, saved);
+    if (rbuf) cudaFree(rbuf);
     if (ts != TRIDI_SUCCESS) return ts;
   } else {
     return TRIDI_ERROR_INVALID_VALUE;

@@ -996,10 +996,29 @@ long padded_rows(long off, int n) { return ((off + n + 3) & ~3L) - (off & ~3L); 
 
 using tridi::RaggedPlan;
 
+namespace tridi {
+namespace {
+tridi_status plan_create(const long* offsets, int num_systems, bool refine, void** plan_out);
+}  // namespace
+}  // namespace tridi
+
 extern "C" {
 
 tridi_status tridi_ragged_plan_create(const long* offsets, int num_systems, void** plan_out) {
-  using namespace tridi;
+  return tridi::plan_create(offsets, num_systems, false, plan_out);
+}
+
+tridi_status tridi_ragged_plan_create_refine(const long* offsets, int num_systems, void** plan_out) {
+  return tridi::plan_create(offsets, num_systems, true, plan_out);
+}
+
+}  // extern "C"
+
+namespace tridi {
+namespace {
+// The work list of a plan (see the file comment); refine: threads per system
+// from the refinement's tuning table where it has an entry.
+tridi_status plan_create(const long* offsets, int num_systems, bool refine, void** plan_out) {
   if (!offsets || num_systems <= 0 || !plan_out) return TRIDI_ERROR_INVALID_VALUE;
   auto* plan = new RaggedPlan();
   plan->num_systems = num_systems;
@@ -1021,8 +1040,9 @@ tridi_status tridi_ragged_plan_create(const long* offsets, int num_systems, void
   for (int s : order) plan->sys.push_back(RagSys{offsets[s], (int)(offsets[s + 1] - offsets[s]), 0});
   // threads per system: the autotuned choice for the system's size bucket,
   // else 32 up to 480 rows, 160 up to 4800, the whole CTA above
-  auto threads_for = [](long n) {
-    const int t = tuned(TRIDI_AUTOTUNE_RAGGED_THREADS, ilog2(n));
+  auto threads_for = [refine](long n) {
+    int t = refine ? tuned(TRIDI_AUTOTUNE_RAGGED_REFINE_THREADS, ilog2(n)) : 0;
+    if (t == 0) t = tuned(TRIDI_AUTOTUNE_RAGGED_THREADS, ilog2(n));
     if (t == 32 || t == kTeamThreads || t == kRagThreads) return t;
     return n <= kWarpMaxRows ? 32 : (n <= kGroupMaxRows ? kTeamThreads : kRagThreads);
   };
@@ -1064,6 +1084,10 @@ tridi_status tridi_ragged_plan_create(const long* offsets, int num_systems, void
   *plan_out = plan;
   return TRIDI_SUCCESS;
 }
+}  // namespace
+}  // namespace tridi
+
+extern "C" {
 
 size_t tridi_ragged_plan_device_bytes(const void* plan) {
   return plan ? static_cast<const RaggedPlan*>(plan)->device_bytes() : 0;

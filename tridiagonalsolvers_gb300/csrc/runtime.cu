@@ -16,7 +16,7 @@ int g_tunable[kTunables] = {};
 int tunable(int key) { return key >= 0 && key < kTunables ? g_tunable[key] : 0; }
 
 namespace {
-constexpr int kTuneTables = 4, kTuneKeys = 32;
+constexpr int kTuneTables = 5, kTuneKeys = 32;
 int g_tuned[kTuneTables][kTuneKeys] = {};
 }  // namespace
 

@@ -463,7 +463,7 @@ class Server {
       for (size_t k = 1; k < r->offsets.size(); ++k)
         offsets.push_back(offsets.back() + r->offsets[k] - r->offsets[k - 1]);
     void* plan = nullptr;
-    tridi_status ts = tridi_ragged_plan_create(offsets.data(), (int)b->systems, &plan);
+    tridi_status ts = tridi_ragged_plan_create_refine(offsets.data(), (int)b->systems, &plan);
     if (ts != TRIDI_SUCCESS) return ts;
     lap(0);
     const long R = pad4(b->rows);

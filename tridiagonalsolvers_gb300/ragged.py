@@ -21,7 +21,10 @@ def padded(total_rows: int) -> int:
 
 
 class RaggedPlan:
-    def __init__(self, offsets, device=None):
+    """refine=True: a plan for RaggedRefiner, with threads per system from the
+    refinement's tuning table ("ragged_refine") where it was tuned."""
+
+    def __init__(self, offsets, device=None, refine: bool = False):
         import torch
 
         off = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
@@ -32,7 +35,8 @@ class RaggedPlan:
         self.total_rows = int(off[-1])
         L = lib()
         h = ctypes.c_void_p()
-        check(L.tridi_ragged_plan_create(off.ctypes.data, self.num_systems, ctypes.byref(h)), "ragged plan")
+        create = L.tridi_ragged_plan_create_refine if refine else L.tridi_ragged_plan_create
+        check(create(off.ctypes.data, self.num_systems, ctypes.byref(h)), "ragged plan")
         self._h = h
         self.items = L.tridi_ragged_plan_items(h)
         nbytes = L.tridi_ragged_plan_device_bytes(h)
