@@ -7,8 +7,10 @@
 //     crpcr_kernel.cu:40-59.
 //   * The remaining rest = n/stride rows (i % stride == stride-1) form the
 //     intermediate system.  log2(rest/2) PCR steps with delta = 1, 2, ...,
-//     rest/4 (neighbours clamped to the first/last row) leave rest/2
-//     independent 2x2 systems (j, j + rest/2), crpcr_kernel.cu:81-119.
+//     rest/4 leave rest/2 independent 2x2 systems (j, j + rest/2),
+//     crpcr_kernel.cu:81-119 (which clamps the neighbours outside the system
+//     to the first / last row; the shuffle paths here use identity rows,
+//     the same values for a[0] = c[n-1] = 0).
 //   * CR back substitution for levels s = stride, ..., 2, crpcr_kernel.cu:127-141.
 //   stride = n/2 is plain CR (cr_kernel.cu), stride = 1 is plain PCR
 //   (pcr_kernel.cu), anything between is crpcr with rest = n/stride.
@@ -122,12 +124,16 @@ __device__ __forceinline__ void pcr_regs_warp(const Row<T> (&r)[K], T (&xr)[K], 
 #pragma unroll
   for (int q = 0; q < R; ++q) y[q] = r[STRIDE * q + STRIDE - 1];
   const int rest = tps * R;
+  // Rows outside the system are identity rows.  The reference clamps those
+  // neighbours to the first / last row instead (pcr_kernel.cu:33-37); with
+  // a[0] = c[n-1] = 0 the rows that reach outside have a zero coupling there
+  // (by induction over the steps), so both give the same values, and the
+  // identity needs no broadcast of the first and last rows.
+  const Row<T> first{T(0), T(1), T(0), T(0)}, last = first;
 #pragma unroll
   for (int e = 0; e < LOGMAX; ++e) {
     const int dl = 1 << e;
     if (4 * dl <= rest) {  // delta = 1 .. rest/4
-      const Row<T> first = shfl_idx(y[0], 0, tps);
-      const Row<T> last = shfl_idx(y[R - 1], tps - 1, tps);
       Row<T> ny[R];
       if (dl < R) {
         Row<T> fromL[R], fromR[R];
@@ -266,14 +272,12 @@ __device__ __forceinline__ void hybrid_solve(Row<T> (&r)[K], T (&xr)[K], int t, 
         if (last_thread) R = C;
         if (((t + 1) & (2 * D - 1)) == 0) C = reduce_row(C, L, R);
       }
-      for (int dl = 1; 4 * dl <= rest; dl *= 2) {
+      for (int dl = 1; 4 * dl <= rest; dl *= 2) {  // outside rows: identity (see pcr_regs_warp)
         const int dd = dl * P;
         Row<T> L = shfl_up(C, dd, tps);
         Row<T> R = shfl_down(C, dd, tps);
-        const Row<T> F = shfl_idx(C, P - 1, tps);
-        const Row<T> Ls = shfl_idx(C, tps - 1, tps);
-        if (j - dl < 0) L = F;
-        if (j + dl > rest - 1) R = Ls;
+        if (j - dl < 0) L = Row<T>{T(0), T(1), T(0), T(0)};
+        if (j + dl > rest - 1) R = Row<T>{T(0), T(1), T(0), T(0)};
         if (on) C = reduce_row(C, L, R);
       }
       const Row<T> pr = shfl_xor(C, tps / 2, tps);
