@@ -124,12 +124,16 @@ __device__ __forceinline__ void pcr_regs_warp(const Row<T> (&r)[K], T (&xr)[K], 
 #pragma unroll
   for (int q = 0; q < R; ++q) y[q] = r[STRIDE * q + STRIDE - 1];
   const int rest = tps * R;
-  // Rows outside the system are identity rows.  The reference clamps those
-  // neighbours to the first / last row instead (pcr_kernel.cu:33-37); with
-  // a[0] = c[n-1] = 0 the rows that reach outside have a zero coupling there
-  // (by induction over the steps), so both give the same values, and the
-  // identity needs no broadcast of the first and last rows.
-  const Row<T> first{T(0), T(1), T(0), T(0)}, last = first;
+  // The system's ends couple to nothing outside it (the gold solver's
+  // a[0] = c[n-1] = 0).  With those two couplings exactly zero, a row whose
+  // neighbour at distance dl lies outside the system has an exactly zero
+  // coupling to it at step dl (by induction over the steps), so any finite
+  // row whose b is a pivot can stand in for the outside one: the shuffles
+  // below hand an out-of-range lane its own row and need no selects.  The
+  // reference clamps to the first / last row instead (pcr_kernel.cu:33-37):
+  // the same values.
+  if (t == 0) y[0].a = T(0);
+  if (t == tps - 1) y[R - 1].c = T(0);
 #pragma unroll
   for (int e = 0; e < LOGMAX; ++e) {
     const int dl = 1 << e;
@@ -144,23 +148,15 @@ __device__ __forceinline__ void pcr_regs_warp(const Row<T> (&r)[K], T (&xr)[K], 
         }
 #pragma unroll
         for (int q = 0; q < R; ++q) {
-          Row<T> L, Rr;
-          if (q >= dl) L = y[(q - dl + R) % R];
-          else L = (t == 0) ? first : fromL[q];
-          if (q + dl < R) Rr = y[(q + dl) % R];
-          else Rr = (t == tps - 1) ? last : fromR[(q + dl - R + R) % R];
+          const Row<T> L = q >= dl ? y[(q - dl + R) % R] : fromL[q];
+          const Row<T> Rr = q + dl < R ? y[(q + dl) % R] : fromR[(q + dl - R + R) % R];
           ny[q] = reduce_row(y[q], L, Rr);
         }
       } else {
         const int ex = dl / R;  // whole threads away
 #pragma unroll
-        for (int q = 0; q < R; ++q) {
-          Row<T> L = shfl_up(y[q], ex, tps);
-          Row<T> Rr = shfl_down(y[q], ex, tps);
-          if (t < ex) L = first;
-          if (t + ex > tps - 1) Rr = last;
-          ny[q] = reduce_row(y[q], L, Rr);
-        }
+        for (int q = 0; q < R; ++q)
+          ny[q] = reduce_row(y[q], shfl_up(y[q], ex, tps), shfl_down(y[q], ex, tps));
       }
 #pragma unroll
       for (int q = 0; q < R; ++q) y[q] = ny[q];
@@ -266,18 +262,21 @@ __device__ __forceinline__ void hybrid_solve(Row<T> (&r)[K], T (&xr)[K], int t, 
     const int j = (t + 1) / P - 1;
     T xC = T(0);
     if constexpr (WARP) {
+      // (the last thread's right neighbour is clamped to itself, as in
+      // cr_kernel.cu:52: shfl_down hands an out-of-range lane its own row)
       for (int D = 1; D < P; D *= 2) {
         const Row<T> L = shfl_up(C, D, tps);
-        Row<T> R = shfl_down(C, D, tps);
-        if (last_thread) R = C;
+        const Row<T> R = shfl_down(C, D, tps);
         if (((t + 1) & (2 * D - 1)) == 0) C = reduce_row(C, L, R);
       }
-      for (int dl = 1; 4 * dl <= rest; dl *= 2) {  // outside rows: identity (see pcr_regs_warp)
+      // PCR with the system's end couplings zeroed: out-of-range lanes get
+      // their own row, which contributes nothing (see pcr_regs_warp)
+      if (on && j == 0) C.a = T(0);
+      if (on && j == rest - 1) C.c = T(0);
+      for (int dl = 1; 4 * dl <= rest; dl *= 2) {
         const int dd = dl * P;
-        Row<T> L = shfl_up(C, dd, tps);
-        Row<T> R = shfl_down(C, dd, tps);
-        if (j - dl < 0) L = Row<T>{T(0), T(1), T(0), T(0)};
-        if (j + dl > rest - 1) R = Row<T>{T(0), T(1), T(0), T(0)};
+        const Row<T> L = shfl_up(C, dd, tps);
+        const Row<T> R = shfl_down(C, dd, tps);
         if (on) C = reduce_row(C, L, R);
       }
       const Row<T> pr = shfl_xor(C, tps / 2, tps);
