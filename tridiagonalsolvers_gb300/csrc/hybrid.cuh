@@ -262,29 +262,49 @@ __device__ __forceinline__ void hybrid_solve(Row<T> (&r)[K], T (&xr)[K], int t, 
     const int j = (t + 1) / P - 1;
     T xC = T(0);
     if constexpr (WARP) {
+      // Levels unrolled to their bound (tps <= 32: P <= 16, rest <= 32, so
+      // at most 4 of each) under warp-uniform conditions; every lane
+      // computes each step and the lanes the step is for keep the result
+      // (selects, no divergent branches).
+      constexpr int kLevels = 4;
       // (the last thread's right neighbour is clamped to itself, as in
       // cr_kernel.cu:52: shfl_down hands an out-of-range lane its own row)
-      for (int D = 1; D < P; D *= 2) {
-        const Row<T> L = shfl_up(C, D, tps);
-        const Row<T> R = shfl_down(C, D, tps);
-        if (((t + 1) & (2 * D - 1)) == 0) C = reduce_row(C, L, R);
+#pragma unroll
+      for (int e = 0; e < kLevels; ++e) {
+        const int D = 1 << e;
+        if (D < P) {
+          const Row<T> L = shfl_up(C, D, tps);
+          const Row<T> R = shfl_down(C, D, tps);
+          const Row<T> N = reduce_row(C, L, R);
+          if (((t + 1) & (2 * D - 1)) == 0) C = N;
+        }
       }
       // PCR with the system's end couplings zeroed: out-of-range lanes get
       // their own row, which contributes nothing (see pcr_regs_warp)
       if (on && j == 0) C.a = T(0);
       if (on && j == rest - 1) C.c = T(0);
-      for (int dl = 1; 4 * dl <= rest; dl *= 2) {
-        const int dd = dl * P;
-        const Row<T> L = shfl_up(C, dd, tps);
-        const Row<T> R = shfl_down(C, dd, tps);
-        if (on) C = reduce_row(C, L, R);
+#pragma unroll
+      for (int e = 0; e < kLevels; ++e) {
+        const int dl = 1 << e;
+        if (4 * dl <= rest) {
+          const int dd = dl * P;
+          const Row<T> L = shfl_up(C, dd, tps);
+          const Row<T> R = shfl_down(C, dd, tps);
+          const Row<T> N = reduce_row(C, L, R);
+          if (on) C = N;
+        }
       }
       const Row<T> pr = shfl_xor(C, tps / 2, tps);
       if (on) xC = (t < tps / 2) ? solve2_upper(C, pr) : solve2_lower(pr, C);
-      for (int D = P / 2; D >= 1; D /= 2) {
-        const T xl = __shfl_up_sync(kFull, xC, D, tps);
-        const T xrr = __shfl_down_sync(kFull, xC, D, tps);
-        if (((t + 1) & (2 * D - 1)) == D) xC = back_row(C, xl, xrr, t == D - 1);
+#pragma unroll
+      for (int e = kLevels - 1; e >= 0; --e) {
+        const int D = 1 << e;
+        if (D < P) {
+          const T xl = __shfl_up_sync(kFull, xC, D, tps);
+          const T xrr = __shfl_down_sync(kFull, xC, D, tps);
+          const T v = back_row(C, xl, xrr, t == D - 1);
+          if (((t + 1) & (2 * D - 1)) == D) xC = v;
+        }
       }
       x_prev = __shfl_up_sync(kFull, xC, 1, tps);
     } else {
