@@ -307,6 +307,84 @@ __device__ __forceinline__ void hybrid_solve(Row<T> (&r)[K], T (&xr)[K], int t, 
         }
       }
       x_prev = __shfl_up_sync(kFull, xC, 1, tps);
+    } else if (P >= 32) {
+      // Block group, levels D = 1..16 inside each warp on shuffles.  Lane 31's
+      // right neighbour at level D is the next warp's lane D-1, final after
+      // level D/2: lane 31 first runs these levels with its own row in that
+      // place, then redoes them once the next warp has exported those rows
+      // (no other lane reads lane 31's rows below level 32: the neighbours
+      // of lane l at level D are lanes l -/+ D <= 30).  The same operands
+      // reach every reduce_row as in the shared-memory form below.
+      const int lane = threadIdx.x & 31, wcta = threadIdx.x >> 5;
+      Row<T>* ex2 = exports + (ct / 32 + 1) * (LOGK > 0 ? LOGK : 1);
+      const Row<T> c0 = C;
+      Row<T> left[5];
+#pragma unroll
+      for (int e = 0; e < 5; ++e) {
+        const int D = 1 << e;
+        left[e] = shfl_up(C, D, 32);
+        const Row<T> N = reduce_row(C, left[e], shfl_down(C, D, 32));
+        if (((lane + 1) & (2 * D - 1)) == 0) C = N;
+      }
+      if (lane < 16 && (lane & (lane + 1)) == 0) ex2[wcta * 5 + (31 - __clz(lane + 1))] = C;
+      consumer_sync(ct);
+      if (lane == 31 && !last_thread) {
+        Row<T> c = c0;
+#pragma unroll
+        for (int e = 0; e < 5; ++e) c = reduce_row(c, left[e], ex2[(wcta + 1) * 5 + e]);
+        C = c;
+      }
+      sc.put(t, C);
+      consumer_sync(ct);
+      for (int D = 32; D < P; D *= 2) {  // across warps
+        if (((t + 1) & (2 * D - 1)) == 0) {
+          const int tr = t + D > tps - 1 ? tps - 1 : t + D;
+          C = reduce_row(C, sc.get(t - D), sc.get(tr));
+          sc.put(t, C);
+        }
+        consumer_sync(ct);
+      }
+      for (int dl = 1; 4 * dl <= rest; dl *= 2) {
+        Row<T> nc = C;
+        if (on) {
+          const int jl = j - dl < 0 ? 0 : j - dl;
+          const int jr = j + dl > rest - 1 ? rest - 1 : j + dl;
+          nc = reduce_row(C, sc.get((jl + 1) * P - 1), sc.get((jr + 1) * P - 1));
+        }
+        consumer_sync(ct);
+        if (on) {
+          C = nc;
+          sc.put(t, C);
+        }
+        consumer_sync(ct);
+      }
+      if (on) {
+        const int pt = t ^ (tps / 2);
+        xC = (t < tps / 2) ? solve2_upper(C, sc.get(pt)) : solve2_lower(sc.get(pt), C);
+        sc.x[t] = xC;
+      }
+      consumer_sync(ct);
+      for (int D = P / 2; D >= 32; D /= 2) {
+        if (((t + 1) & (2 * D - 1)) == D) {
+          const T xl = (t - D >= 0) ? sc.x[t - D] : T(0);
+          xC = back_row(C, xl, sc.x[t + D], t == D - 1);
+          sc.x[t] = xC;
+        }
+        consumer_sync(ct);
+      }
+      // levels D = 16..1 inside each warp; lane D-1's left neighbour is the
+      // previous warp's lane 31, whose x is in sc.x
+      const T xpw = (t - lane > 0) ? sc.x[t - lane - 1] : T(0);
+#pragma unroll
+      for (int e = 4; e >= 0; --e) {
+        const int D = 1 << e;
+        const T xu = __shfl_up_sync(kFull, xC, D, 32);
+        const T xrr = __shfl_down_sync(kFull, xC, D, 32);
+        const T v = back_row(C, lane < D ? xpw : xu, xrr, t == D - 1);
+        if (((lane + 1) & (2 * D - 1)) == D) xC = v;
+      }
+      const T xu = __shfl_up_sync(kFull, xC, 1, 32);
+      x_prev = lane == 0 ? xpw : xu;
     } else {
       sc.put(t, C);
       consumer_sync(ct);
@@ -372,14 +450,15 @@ __device__ __forceinline__ void hybrid_solve(Row<T> (&r)[K], T (&xr)[K], int t, 
 template <class T>
 struct HybridSmem {
   // [full[S] | empty[S]] barriers (128 B), S stages of 4*G*n T, then the
-  // block-path scratch: G groups * 5 * rows T, then exports.
+  // block-path scratch: G groups * 5 * rows T, then exports (per warp: its
+  // lane 0's rows of the in-thread levels, then 5 rows of the in-warp levels).
   static __host__ __device__ size_t barrier_bytes() { return 128; }
   static __host__ __device__ size_t stage_elems(int G, int n) { return (size_t)4 * G * n; }
   static __host__ __device__ size_t bytes(int stages, int G, int n, int rows, bool warp, int ct, int logk) {
     size_t s = barrier_bytes() + (size_t)stages * stage_elems(G, n) * sizeof(T);
     if (!warp) {
       s += (size_t)G * 5 * rows * sizeof(T);
-      s += (size_t)(ct / 32 + 1) * (logk > 0 ? logk : 1) * sizeof(Row<T>);
+      s += (size_t)(ct / 32 + 1) * ((logk > 0 ? logk : 1) + 5) * sizeof(Row<T>);
     }
     return s;
   }
