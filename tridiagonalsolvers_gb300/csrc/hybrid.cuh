@@ -134,29 +134,35 @@ __device__ __forceinline__ void pcr_regs_warp(const Row<T> (&r)[K], T (&xr)[K], 
   // the same values.
   if (t == 0) y[0].a = T(0);
   if (t == tps - 1) y[R - 1].c = T(0);
+  // Every row is the divisor of its two neighbours at each step: its owner
+  // forms 1/b once and hands (a, 1/b, c, d) to them (reduce_row_inv), one
+  // reciprocal per row and step instead of two.
 #pragma unroll
   for (int e = 0; e < LOGMAX; ++e) {
     const int dl = 1 << e;
     if (4 * dl <= rest) {  // delta = 1 .. rest/4
+      Row<T> w[R];
+#pragma unroll
+      for (int q = 0; q < R; ++q) w[q] = Row<T>{y[q].a, tdiv(T(1), y[q].b), y[q].c, y[q].d};
       Row<T> ny[R];
       if (dl < R) {
         Row<T> fromL[R], fromR[R];
 #pragma unroll
         for (int q = 0; q < R; ++q) {
-          if (q < dl) fromL[q] = shfl_up(y[(R - dl + q) % R], 1, tps);
-          if (q < dl) fromR[q] = shfl_down(y[q % R], 1, tps);
+          if (q < dl) fromL[q] = shfl_up(w[(R - dl + q) % R], 1, tps);
+          if (q < dl) fromR[q] = shfl_down(w[q % R], 1, tps);
         }
 #pragma unroll
         for (int q = 0; q < R; ++q) {
-          const Row<T> L = q >= dl ? y[(q - dl + R) % R] : fromL[q];
-          const Row<T> Rr = q + dl < R ? y[(q + dl) % R] : fromR[(q + dl - R + R) % R];
-          ny[q] = reduce_row(y[q], L, Rr);
+          const Row<T> L = q >= dl ? w[(q - dl + R) % R] : fromL[q];
+          const Row<T> Rr = q + dl < R ? w[(q + dl) % R] : fromR[(q + dl - R + R) % R];
+          ny[q] = reduce_row_inv(y[q], L, Rr);
         }
       } else {
         const int ex = dl / R;  // whole threads away
 #pragma unroll
         for (int q = 0; q < R; ++q)
-          ny[q] = reduce_row(y[q], shfl_up(y[q], ex, tps), shfl_down(y[q], ex, tps));
+          ny[q] = reduce_row_inv(y[q], shfl_up(w[q], ex, tps), shfl_down(w[q], ex, tps));
       }
 #pragma unroll
       for (int q = 0; q < R; ++q) y[q] = ny[q];

@@ -42,6 +42,21 @@ __device__ __forceinline__ Row<T> reduce_row(const Row<T>& me, const Row<T>& L, 
   return o;
 }
 
+// The same elimination with the neighbours' reciprocals already formed:
+// L.b and R.b hold 1/b of the neighbour rows (PCR, where each row divides
+// both of its neighbours at a step).
+template <class T>
+__device__ __forceinline__ Row<T> reduce_row_inv(const Row<T>& me, const Row<T>& L, const Row<T>& R) {
+  T tmp1 = me.a * L.b;
+  T tmp2 = me.c * R.b;
+  Row<T> o;
+  o.b = me.b - L.c * tmp1 - R.a * tmp2;
+  o.d = me.d - L.d * tmp1 - R.d * tmp2;
+  o.a = -L.a * tmp1;
+  o.c = -R.c * tmp2;
+  return o;
+}
+
 // The 2x2 solve that closes CR / PCR (cr_kernel.cu:65-69, pcr_kernel.cu:67-71):
 // unknown 1 is the upper equation (r1), unknown 2 the lower (r2).
 template <class T>
