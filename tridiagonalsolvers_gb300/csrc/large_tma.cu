@@ -174,28 +174,48 @@ __global__ void __launch_bounds__(32 * (kLtWarps + 1), 1)
     const long rem = p.n - r0;
     const int kr = rem <= 0 ? 0 : (rem < kLtChunk ? (int)rem : kLtChunk);
     ChunkSummary<float> cs;
-    if (kr > 0) {
-      const long o = j * p.m + sys;
+    if constexpr (BACK) {
+      // The eliminated column stays in registers and the stage goes back to
+      // the producer before the back substitution (and before the wait for
+      // the separators, whose loads overlap the elimination), so a stage is
+      // held for the elimination only.
+      float cp[kLtChunk], ap[kLtChunk], dp[kLtChunk];
       float sj = 0.f, sl = 0.f;
-      if constexpr (BACK) {  // the separators' loads overlap the elimination
+      if (kr > 0) {
+        const long o = j * p.m + sys;
         sj = p.sol[o];
         sl = j > 0 ? p.sol[o - p.m] : 0.f;
+        const bool first = j == 0;
+        float cprev = 0.f, aprev = 0.f, dprev = 0.f;
+#pragma unroll
+        for (int i = 0; i < kLtChunk - 1; ++i) {
+          if (i < kr - 1) {
+            const int oo = i * kTileCols;
+            const float a = (i == 0 && first) ? 0.f : sa[oo];
+            const float inv = tdiv(1.f, sb[oo] - a * cprev);
+            cp[i] = sc[oo] * inv;
+            ap[i] = (i == 0 ? a : -a * aprev) * inv;
+            dp[i] = (sd[oo] - a * dprev) * inv;
+            cprev = cp[i]; aprev = ap[i]; dprev = dp[i];
+          }
+        }
       }
-      column_eliminate(cs, kr, j == 0, j == p.P - 1, sa, sb, sc, sd);
-      if constexpr (BACK) {
+      release_stage(&empty[s]);
+      if (kr > 0) {
         float* gx = p.x + r0 * p.m + sys;
         gx[(long)(kr - 1) * p.m] = sj;
         float xn = sj;
 #pragma unroll
         for (int i = kLtChunk - 2; i >= 0; --i) {
           if (i <= kr - 2) {
-            const int oo = i * kTileCols;
-            xn = sd[oo] - sc[oo] * xn - sa[oo] * sl;
+            xn = dp[i] - cp[i] * xn - ap[i] * sl;
             gx[(long)i * p.m] = xn;
           }
         }
       }
+      continue;
     }
+    if (kr > 0) column_eliminate(cs, kr, j == 0, j == p.P - 1, sa, sb, sc, sd);
     if constexpr (!BACK) {
       // separator rows: warp w < 7 takes the next chunk's first row from warp
       // w + 1 of the same tile; a tile's last chunk and its first chunk go to
