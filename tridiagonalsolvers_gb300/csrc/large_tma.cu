@@ -72,49 +72,49 @@ __device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* map, 
       : "memory");
 }
 
-// Chunk elimination of one lane's column (rows 0..k-1 at stride 32 words),
-// in place, and its interface (partition.cuh's Chunk summary).
-__device__ __forceinline__ void column_eliminate(ChunkSummary<float>& cs, int k, bool first, bool last,
-                                                 float* __restrict__ sa, const float* __restrict__ sb,
-                                                 float* __restrict__ sc, float* __restrict__ sd) {
-  float cprev = 0.f, aprev = 0.f, dprev = 0.f;
+// Forward elimination of one lane's column (rows 0..k-2 at stride 32 words)
+// into registers: the normalised c', a', d' of every interior row.  The
+// stage can go back to the producer as soon as this (and the read of the
+// separator row) is done.
+__device__ __forceinline__ void column_forward(int k, bool first, const float* __restrict__ sa,
+                                               const float* __restrict__ sb, const float* __restrict__ sc,
+                                               const float* __restrict__ sd, float (&cp)[kLtChunk],
+                                               float (&ap)[kLtChunk], float (&dp)[kLtChunk], float& cprev,
+                                               float& aprev, float& dprev) {
+  cprev = 0.f; aprev = 0.f; dprev = 0.f;
 #pragma unroll
   for (int i = 0; i < kLtChunk - 1; ++i) {
     if (i < k - 1) {
       const int o = i * kTileCols;
       const float a = (i == 0 && first) ? 0.f : sa[o];
       const float inv = tdiv(1.f, sb[o] - a * cprev);
-      const float cn = sc[o] * inv;
-      const float an = (i == 0 ? a : -a * aprev) * inv;
-      const float dn = (sd[o] - a * dprev) * inv;
-      sa[o] = an; sc[o] = cn; sd[o] = dn;
-      cprev = cn; aprev = an; dprev = dn;
+      cp[i] = sc[o] * inv;
+      ap[i] = (i == 0 ? a : -a * aprev) * inv;
+      dp[i] = (sd[o] - a * dprev) * inv;
+      cprev = cp[i]; aprev = ap[i]; dprev = dp[i];
     }
   }
+}
+
+// The chunk's interface (partition.cuh's Chunk summary) from its eliminated
+// rows in registers (last interior row: cl, al, dl).
+__device__ __forceinline__ void column_summary(ChunkSummary<float>& cs, int k, const float (&cp)[kLtChunk],
+                                               const float (&ap)[kLtChunk], const float (&dp)[kLtChunk], float cl,
+                                               float al, float dl) {
   float D = 0.f, C = -1.f, A = 0.f;
 #pragma unroll
   for (int i = kLtChunk - 2; i >= 0; --i) {
     if (i <= k - 2) {
-      const int o = i * kTileCols;
-      const float c = sc[o];
-      D = sd[o] - c * D;
-      C = -c * C;
-      A = sa[o] - c * A;
+      D = dp[i] - cp[i] * D;
+      C = -cp[i] * C;
+      A = ap[i] - cp[i] * A;
     }
   }
   cs.fD = D; cs.fC = C; cs.fA = A;
   if (k >= 2) {
-    cs.lD = dprev; cs.lC = cprev; cs.lA = aprev;
+    cs.lD = dl; cs.lC = cl; cs.lA = al;
   } else {
     cs.lD = 0.f; cs.lC = 0.f; cs.lA = -1.f;
-  }
-  if (k >= 1) {
-    const int o = (k - 1) * kTileCols;
-    cs.sep = Row<float>{sa[o], sb[o], sc[o], sd[o]};
-    if (k == 1 && first) cs.sep.a = 0.f;
-    if (last) cs.sep.c = 0.f;
-  } else {
-    cs.sep = Row<float>{0.f, 1.f, 0.f, 0.f};
   }
 }
 
@@ -174,33 +174,29 @@ __global__ void __launch_bounds__(32 * (kLtWarps + 1), 1)
     const long rem = p.n - r0;
     const int kr = rem <= 0 ? 0 : (rem < kLtChunk ? (int)rem : kLtChunk);
     ChunkSummary<float> cs;
-    if constexpr (BACK) {
-      // The eliminated column stays in registers and the stage goes back to
-      // the producer before the back substitution (and before the wait for
-      // the separators, whose loads overlap the elimination), so a stage is
-      // held for the elimination only.
-      float cp[kLtChunk], ap[kLtChunk], dp[kLtChunk];
-      float sj = 0.f, sl = 0.f;
-      if (kr > 0) {
+    // The eliminated column stays in registers and the stage goes back to
+    // the producer right after the elimination, so a stage is held for the
+    // elimination only (not for the separator wait and back substitution,
+    // nor for the interface exchange).
+    float cp[kLtChunk], ap[kLtChunk], dp[kLtChunk];
+    float cl = 0.f, al = 0.f, dl = 0.f;
+    float sj = 0.f, sl = 0.f;
+    if (kr > 0) {
+      if constexpr (BACK) {  // the separators' loads overlap the elimination
         const long o = j * p.m + sys;
         sj = p.sol[o];
         sl = j > 0 ? p.sol[o - p.m] : 0.f;
-        const bool first = j == 0;
-        float cprev = 0.f, aprev = 0.f, dprev = 0.f;
-#pragma unroll
-        for (int i = 0; i < kLtChunk - 1; ++i) {
-          if (i < kr - 1) {
-            const int oo = i * kTileCols;
-            const float a = (i == 0 && first) ? 0.f : sa[oo];
-            const float inv = tdiv(1.f, sb[oo] - a * cprev);
-            cp[i] = sc[oo] * inv;
-            ap[i] = (i == 0 ? a : -a * aprev) * inv;
-            dp[i] = (sd[oo] - a * dprev) * inv;
-            cprev = cp[i]; aprev = ap[i]; dprev = dp[i];
-          }
-        }
       }
-      release_stage(&empty[s]);
+      column_forward(kr, j == 0, sa, sb, sc, sd, cp, ap, dp, cl, al, dl);
+      if constexpr (!BACK) {
+        const int o = (kr - 1) * kTileCols;
+        cs.sep = Row<float>{sa[o], sb[o], sc[o], sd[o]};
+        if (kr == 1 && j == 0) cs.sep.a = 0.f;
+        if (j == p.P - 1) cs.sep.c = 0.f;
+      }
+    }
+    release_stage(&empty[s]);
+    if constexpr (BACK) {
       if (kr > 0) {
         float* gx = p.x + r0 * p.m + sys;
         gx[(long)(kr - 1) * p.m] = sj;
@@ -215,7 +211,7 @@ __global__ void __launch_bounds__(32 * (kLtWarps + 1), 1)
       }
       continue;
     }
-    if (kr > 0) column_eliminate(cs, kr, j == 0, j == p.P - 1, sa, sb, sc, sd);
+    if (kr > 0) column_summary(cs, kr, cp, ap, dp, cl, al, dl);
     if constexpr (!BACK) {
       // separator rows: warp w < 7 takes the next chunk's first row from warp
       // w + 1 of the same tile; a tile's last chunk and its first chunk go to
@@ -243,7 +239,6 @@ __global__ void __launch_bounds__(32 * (kLtWarps + 1), 1)
         }
       }
     }
-    release_stage(&empty[s]);
   }
 }
 
