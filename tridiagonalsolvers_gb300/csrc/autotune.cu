@@ -175,6 +175,10 @@ extern "C" tridi_status tridi_autotune(int table, long key, long sample, tridi_s
     long hi = (2L << k) - 1;
     if (k > 14) return TRIDI_ERROR_UNSUPPORTED_SIZE;
     if (hi > 24480) hi = 24480;
+    // above the team limit every candidate gives a system the whole CTA: time
+    // only the sizes the choice decides (for [8192, 16384): 8192 .. ~8950)
+    const long cap = ragged_team_max_rows() - 8;
+    if (lo <= cap && hi > cap) hi = cap;
     // sizes spread evenly over the bucket, enough systems for `sample` rows
     std::vector<long> off(1, 0);
     for (long s = 0; off.back() < sample && s < (1L << 22); ++s)

@@ -992,6 +992,8 @@ namespace {
 long padded_rows(long off, int n) { return ((off + n + 3) & ~3L) - (off & ~3L); }
 }  // namespace
 
+long ragged_team_max_rows() { return ring_rows(kRefineDF); }
+
 }  // namespace tridi
 
 using tridi::RaggedPlan;
@@ -1046,7 +1048,7 @@ tridi_status plan_create(const long* offsets, int num_systems, bool refine, void
     if (t == 32 || t == kTeamThreads || t == kRagThreads) return t;
     return n <= kWarpMaxRows ? 32 : (n <= kGroupMaxRows ? kTeamThreads : kRagThreads);
   };
-  constexpr long kPackCap = ring_rows(kRefineDF);  // a team item fits the ring of every mode
+  const long kPackCap = ragged_team_max_rows();  // a team item fits the ring of every mode
   std::vector<RagItem> cta_items, team_items;      // CTA-wide items go first (phase 1 of the kernel)
   int i = 0;
   while (i < num_systems) {

@@ -35,6 +35,9 @@ int tunable(int key);
 // and key (log2 of the system size, or of the size bucket), the chosen value;
 // 0 where nothing was tuned.
 int tuned(int table, int log2key);
+// Ragged plans: the largest padded row count a warp or team item may hold
+// (larger systems always take a whole CTA, whatever the threads table says).
+long ragged_team_max_rows();
 
 inline int ilog2(long v) {
   int k = 0;
