@@ -135,18 +135,19 @@ __device__ __forceinline__ void pcr_regs_warp(const Row<T> (&r)[K], T (&xr)[K], 
   if (t == 0) y[0].a = T(0);
   if (t == tps - 1) y[R - 1].c = T(0);
   // Every row is the divisor of its two neighbours at each step: its owner
-  // forms 1/b once and hands (a, 1/b, c, d) to them (reduce_row_inv), one
-  // reciprocal per row and step instead of two.
+  // divides it by its diagonal once and hands (a/b, c/b, d/b) to them
+  // (reduce_row_nrm): one reciprocal per row and step instead of two, three
+  // shuffled values per neighbour instead of four.
 #pragma unroll
   for (int e = 0; e < LOGMAX; ++e) {
     const int dl = 1 << e;
     if (4 * dl <= rest) {  // delta = 1 .. rest/4
-      Row<T> w[R];
+      NRow<T> w[R];
 #pragma unroll
-      for (int q = 0; q < R; ++q) w[q] = Row<T>{y[q].a, tdiv(T(1), y[q].b), y[q].c, y[q].d};
+      for (int q = 0; q < R; ++q) w[q] = normalize_row(y[q]);
       Row<T> ny[R];
       if (dl < R) {
-        Row<T> fromL[R], fromR[R];
+        NRow<T> fromL[R], fromR[R];
 #pragma unroll
         for (int q = 0; q < R; ++q) {
           if (q < dl) fromL[q] = shfl_up(w[(R - dl + q) % R], 1, tps);
@@ -154,15 +155,15 @@ __device__ __forceinline__ void pcr_regs_warp(const Row<T> (&r)[K], T (&xr)[K], 
         }
 #pragma unroll
         for (int q = 0; q < R; ++q) {
-          const Row<T> L = q >= dl ? w[(q - dl + R) % R] : fromL[q];
-          const Row<T> Rr = q + dl < R ? w[(q + dl) % R] : fromR[(q + dl - R + R) % R];
-          ny[q] = reduce_row_inv(y[q], L, Rr);
+          const NRow<T> L = q >= dl ? w[(q - dl + R) % R] : fromL[q];
+          const NRow<T> Rr = q + dl < R ? w[(q + dl) % R] : fromR[(q + dl - R + R) % R];
+          ny[q] = reduce_row_nrm(y[q], L, Rr);
         }
       } else {
         const int ex = dl / R;  // whole threads away
 #pragma unroll
         for (int q = 0; q < R; ++q)
-          ny[q] = reduce_row_inv(y[q], shfl_up(w[q], ex, tps), shfl_down(w[q], ex, tps));
+          ny[q] = reduce_row_nrm(y[q], shfl_up(w[q], ex, tps), shfl_down(w[q], ex, tps));
       }
 #pragma unroll
       for (int q = 0; q < R; ++q) y[q] = ny[q];

@@ -42,18 +42,28 @@ __device__ __forceinline__ Row<T> reduce_row(const Row<T>& me, const Row<T>& L, 
   return o;
 }
 
-// The same elimination with the neighbours' reciprocals already formed:
-// L.b and R.b hold 1/b of the neighbour rows (PCR, where each row divides
-// both of its neighbours at a step).
+// A row divided by its diagonal: (a/b, c/b, d/b).  In PCR every row is the
+// divisor of both its neighbours at a step, so its owner divides once and
+// hands them these three values (three shuffles instead of four).
 template <class T>
-__device__ __forceinline__ Row<T> reduce_row_inv(const Row<T>& me, const Row<T>& L, const Row<T>& R) {
-  T tmp1 = me.a * L.b;
-  T tmp2 = me.c * R.b;
+struct NRow {
+  T a, c, d;
+};
+template <class T>
+__device__ __forceinline__ NRow<T> normalize_row(const Row<T>& r) {
+  const T ib = tdiv(T(1), r.b);
+  return {r.a * ib, r.c * ib, r.d * ib};
+}
+
+// reduce_row with the neighbours given as normalised rows:
+// me - (me.a) L - (me.c) R, the same elimination up to rounding order.
+template <class T>
+__device__ __forceinline__ Row<T> reduce_row_nrm(const Row<T>& me, const NRow<T>& L, const NRow<T>& R) {
   Row<T> o;
-  o.b = me.b - L.c * tmp1 - R.a * tmp2;
-  o.d = me.d - L.d * tmp1 - R.d * tmp2;
-  o.a = -L.a * tmp1;
-  o.c = -R.c * tmp2;
+  o.b = me.b - me.a * L.c - me.c * R.a;
+  o.d = me.d - me.a * L.d - me.c * R.d;
+  o.a = -me.a * L.a;
+  o.c = -me.c * R.c;
   return o;
 }
 
@@ -80,6 +90,17 @@ __device__ __forceinline__ T back_row(const Row<T>& r, T xl, T xr, bool first) {
 
 // ---- warp shuffles of rows -------------------------------------------------
 constexpr unsigned kFull = 0xffffffffu;
+
+template <class T>
+__device__ __forceinline__ NRow<T> shfl_up(const NRow<T>& v, int delta, int width) {
+  return {__shfl_up_sync(kFull, v.a, delta, width), __shfl_up_sync(kFull, v.c, delta, width),
+          __shfl_up_sync(kFull, v.d, delta, width)};
+}
+template <class T>
+__device__ __forceinline__ NRow<T> shfl_down(const NRow<T>& v, int delta, int width) {
+  return {__shfl_down_sync(kFull, v.a, delta, width), __shfl_down_sync(kFull, v.c, delta, width),
+          __shfl_down_sync(kFull, v.d, delta, width)};
+}
 
 template <class T>
 __device__ __forceinline__ Row<T> shfl_up(const Row<T>& v, int delta, int width) {
