@@ -169,11 +169,18 @@ __device__ __forceinline__ void pcr_regs_warp(const Row<T> (&r)[K], T (&xr)[K], 
       for (int q = 0; q < R; ++q) y[q] = ny[q];
     }
   }
-  // 2x2 systems (j, j + rest/2): same local slot, thread t ^ tps/2.
+  // 2x2 systems (j, j + rest/2): same local slot, thread t ^ tps/2.  Each
+  // side needs the partner's d/b and its coupling to this side over b (c/b
+  // from the upper row, a/b from the lower): x = (d - k d') / (b - k k'),
+  // k this row's coupling to the partner.
+  const bool upper = t < tps / 2;
 #pragma unroll
   for (int q = 0; q < R; ++q) {
-    const Row<T> p = shfl_xor(y[q], tps / 2, tps);
-    xr[STRIDE * q + STRIDE - 1] = (t < tps / 2) ? solve2_upper(y[q], p) : solve2_lower(p, y[q]);
+    const NRow<T> w = normalize_row(y[q]);
+    const T pd = __shfl_xor_sync(kFull, w.d, tps / 2, tps);
+    const T pk = __shfl_xor_sync(kFull, upper ? w.c : w.a, tps / 2, tps);
+    const T k = upper ? y[q].c : y[q].a;
+    xr[STRIDE * q + STRIDE - 1] = tdiv(y[q].d - k * pd, y[q].b - k * pk);
   }
 }
 
