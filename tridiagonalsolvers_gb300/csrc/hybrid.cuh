@@ -195,35 +195,51 @@ __device__ __forceinline__ void pcr_regs_block(const Row<T> (&r)[K], T (&xr)[K],
   auto at = [tps](int j) { return (j % R) * tps + j / R; };
   Row<T> y[R];
 #pragma unroll
-  for (int q = 0; q < R; ++q) {
-    y[q] = r[STRIDE * q + STRIDE - 1];
-    sc.put(q * tps + t, y[q]);
-  }
+  for (int q = 0; q < R; ++q) y[q] = r[STRIDE * q + STRIDE - 1];
+  // end couplings zeroed, normalised rows exchanged: as in pcr_regs_warp
+  // (the clamped neighbours of the rows near the ends then contribute
+  // exactly nothing; three words per row in shared memory instead of four)
+  if (t == 0) y[0].a = T(0);
+  if (t == tps - 1) y[R - 1].c = T(0);
   const int rest = tps * R;
-  consumer_sync(ct);
   for (int dl = 1; 4 * dl <= rest; dl *= 2) {
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const NRow<T> w = normalize_row(y[q]);
+      sc.a[q * tps + t] = w.a;
+      sc.c[q * tps + t] = w.c;
+      sc.d[q * tps + t] = w.d;
+    }
+    consumer_sync(ct);
     Row<T> ny[R];
 #pragma unroll
     for (int q = 0; q < R; ++q) {
       const int j = t * R + q;
-      const int jl = j - dl < 0 ? 0 : j - dl;
-      const int jr = j + dl > rest - 1 ? rest - 1 : j + dl;
-      ny[q] = reduce_row(y[q], sc.get(at(jl)), sc.get(at(jr)));
+      const int ol = at(j - dl < 0 ? 0 : j - dl);
+      const int orr = at(j + dl > rest - 1 ? rest - 1 : j + dl);
+      ny[q] = reduce_row_nrm(y[q], NRow<T>{sc.a[ol], sc.c[ol], sc.d[ol]}, NRow<T>{sc.a[orr], sc.c[orr], sc.d[orr]});
     }
     consumer_sync(ct);
 #pragma unroll
-    for (int q = 0; q < R; ++q) {
-      y[q] = ny[q];
-      sc.put(q * tps + t, y[q]);
-    }
-    consumer_sync(ct);
+    for (int q = 0; q < R; ++q) y[q] = ny[q];
   }
+  // 2x2 systems (j, j + rest/2): x = (d - k d') / (b - k k') with the
+  // partner's normalised d and coupling to this row (see pcr_regs_warp)
   const int half = rest / 2;
 #pragma unroll
   for (int q = 0; q < R; ++q) {
     const int j = t * R + q;
-    xr[STRIDE * q + STRIDE - 1] =
-        (j < half) ? solve2_upper(y[q], sc.get(at(j + half))) : solve2_lower(sc.get(at(j - half)), y[q]);
+    const NRow<T> w = normalize_row(y[q]);
+    sc.a[q * tps + t] = j < half ? w.c : w.a;
+    sc.d[q * tps + t] = w.d;
+  }
+  consumer_sync(ct);
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int j = t * R + q;
+    const int o = at(j < half ? j + half : j - half);
+    const T k = j < half ? y[q].c : y[q].a;
+    xr[STRIDE * q + STRIDE - 1] = tdiv(y[q].d - k * sc.d[o], y[q].b - k * sc.a[o]);
   }
 }
 
