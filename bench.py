@@ -305,7 +305,8 @@ def run_gpu(args):
         cands = [("cr", lambda: lib.tridi_cr_f32(*ptrs, N, M, sp)),
                  ("crNBC", lambda: lib.tridi_cr_nbc_f32(*ptrs, N, M, sp)),
                  ("pcr", lambda: lib.tridi_pcr_f32(*ptrs, N, M, sp)),
-                 ("partition", lambda: lib.tridi_solve_f32(*ptrs, N, M, sp))]
+                 ("partition", lambda: lib.tridi_solve_f32(*ptrs, N, M, sp)),
+                 ("pcrGauss", lambda: lib.tridi_pcr_thomas_f32(*ptrs, N, M, 0, sp))]
         rest = 2
         while rest <= N // 2:
             cands.append((f"crpcr_rest{rest}", (lambda r: lambda: lib.tridi_crpcr_f32(*ptrs, N, M, r, sp))(rest)))

@@ -137,7 +137,9 @@ tridi_status tridi_crpcr_nbc_f64(const double *a, const double *b, const double 
    subsystems (a power of two, 1 <= g <= n) solved by Thomas after log2(g) PCR
    steps.  Exact for every g (the reference's step table is exact only when
    g = 2^it).  gaussian = 0: the autotuned g for n (TRIDI_AUTOTUNE_PCR_THOMAS_SPLIT),
-   else one chain per thread of the system.  Any 1 <= n <= 4096. */
+   else n/2 for power-of-two n (else one chain per thread of the system).
+   g >= n/2 on power-of-two n runs the register PCR kernels (log2(n/2) PCR
+   steps leave exactly the 2-row chains PCR closes with).  Any 1 <= n <= 4096. */
 tridi_status tridi_pcr_thomas_f32(const float *a, const float *b, const float *c, const float *d, float *x, int n,
                                   int num_systems, int gaussian, tridi_stream_t stream);
 tridi_status tridi_pcr_thomas_f64(const double *a, const double *b, const double *c, const double *d, double *x,

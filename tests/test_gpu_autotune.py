@@ -79,7 +79,7 @@ def test_table_round_trip(tmp_path, cuda):
     assert t["ragged"]["64"] == 160 and t["crpcr_rest"]["256"] == 16 and t["pcr_thomas"]["128"] == 8
 
 
-@pytest.mark.parametrize("n", [64, 512])
+@pytest.mark.parametrize("n", [64, 512, 1024, 2048])
 def test_tune_cr_rows_then_solve(cuda, n):
     import torch
 
@@ -90,10 +90,15 @@ def test_tune_cr_rows_then_solve(cuda, n):
     assert autotune.table()["cr_rows"][str(n)] == rows
     a, b, c, d = workloads.dominant(96, n, seed=12)
     t = [torch.from_numpy(v).to(cuda) for v in (a, b, c, d)]
-    for rr in (4, 8, 16):  # every instantiated shape gives a correct CR
+    for rr in (4, 8, 16):  # every instantiated shape gives a correct CR and CR-PCR
+        if n // rr > 256:
+            continue
         autotune.set_table({"cr_rows": {str(n): rr}})
         x = tg.cr(*t).cpu().numpy()
         assert gold.rel_residual(a, b, c, d, x).max() <= RES_TOL[np.float32], rr
+        for rest in (4, 32):  # rows left after CR: one per warp, or several per warp
+            x = tg.crpcr(*t, rest).cpu().numpy()
+            assert gold.rel_residual(a, b, c, d, x).max() <= RES_TOL[np.float32], (rr, rest)
 
 
 def test_tune_ragged_refine_buckets_and_refine(cuda):

@@ -39,10 +39,11 @@ struct PTParams {
   unsigned* status;
 };
 
-// PCR rows per thread kept in registers between the read and write phases.
+// PCR rows per thread kept in registers between the read and write phases
+// (at most; ROWS, the kernel's template argument, is the launch's bound).
 constexpr int kPTMaxRows = 16;
 
-template <class T, int MAXT>
+template <class T, int MAXT, int ROWS>
 __global__ void __launch_bounds__(MAXT) pcr_thomas_kernel(PTParams p) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
@@ -124,9 +125,9 @@ __global__ void __launch_bounds__(MAXT) pcr_thomas_kernel(PTParams p) {
 
     // ---- log2(g) PCR steps, delta = 1, 2, ..., g/2 ----
     for (int dl = 1; dl < p.g; dl *= 2) {
-      Row<T> nr[kPTMaxRows];
+      Row<T> nr[ROWS];
 #pragma unroll
-      for (int q = 0; q < kPTMaxRows; ++q) {
+      for (int q = 0; q < ROWS; ++q) {
         const int i = t + q * tps;
         if (q < rows && i < n) {
           const int il = i - dl < 0 ? 0 : i - dl;
@@ -137,7 +138,7 @@ __global__ void __launch_bounds__(MAXT) pcr_thomas_kernel(PTParams p) {
       }
       consumer_sync(ct);
 #pragma unroll
-      for (int q = 0; q < kPTMaxRows; ++q) {
+      for (int q = 0; q < ROWS; ++q) {
         const int i = t + q * tps;
         if (q < rows && i < n) {
           wa[i] = nr[q].a; wb[i] = nr[q].b; wc[i] = nr[q].c; wd[i] = nr[q].d;
@@ -172,6 +173,9 @@ __global__ void __launch_bounds__(MAXT) pcr_thomas_kernel(PTParams p) {
   }
 }
 
+template <class T>
+tridi_status hybrid_solve_device(const T*, const T*, const T*, const T*, T*, int, int, int, tridi_stream_t);
+
 namespace {
 template <class T>
 size_t pt_smem(int S, int G, int n) {
@@ -185,10 +189,13 @@ tridi_status pcr_thomas_device(const T* a, const T* b, const T* c, const T* d, T
   if (!a || !b || !c || !d || !x || m <= 0) return TRIDI_ERROR_INVALID_VALUE;
   const int nmax = 4096;
   if (n < 1 || n > nmax || g < 0) return TRIDI_ERROR_UNSUPPORTED_SIZE;
-  if (g == 0) {  // the autotuned split for this n, else one chain per thread of the system
+  const bool pcr_shape = is_pow2(n) && n >= 4 && n <= (sizeof(T) == 4 ? 4096 : 2048);
+  if (g == 0) {  // the autotuned split for this n, else n/2 (power-of-two n), else one chain per thread
     const int t = is_pow2(n) ? tuned(TRIDI_AUTOTUNE_PCR_THOMAS_SPLIT, ilog2(n)) : 0;
     if (t > 0 && is_pow2(t) && t <= n) {
       g = t;
+    } else if (pcr_shape) {
+      g = n / 2;
     } else {
       int tp = 32;
       while (tp < 256 && tp < n) tp *= 2;
@@ -197,6 +204,10 @@ tridi_status pcr_thomas_device(const T* a, const T* b, const T* c, const T* d, T
     }
   }
   if (!is_pow2(g) || g > n) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  // g >= n/2: after log2(n/2) PCR steps the chains are the 2-row systems
+  // (j, j + n/2) that close PCR (g = n: one more step decouples every row,
+  // the same solution), so the register PCR kernels solve it.
+  if (pcr_shape && g >= n / 2) return hybrid_solve_device<T>(a, b, c, d, x, n, m, 1, stream);
   const DeviceInfo* dev = current_device();
   if (!dev) return TRIDI_ERROR_CUDA;
   PTParams p{};
@@ -206,15 +217,17 @@ tridi_status pcr_thomas_device(const T* a, const T* b, const T* c, const T* d, T
   while ((1 << steps) < g) ++steps;
   p.steps = steps;
   // threads per system: every PCR row of a thread stays in registers between
-  // the read and write phases, so rows per thread <= kPTMaxRows.
-  const int max_rows = kPTMaxRows;
+  // the read and write phases; up to 4 rows a thread (8, 16 at n = 2048,
+  // 4096), so small systems take one or two warps and a CTA holds several
+  // systems, whose steps share its barriers, with two CTAs per SM.
   int tps = 32;
-  while (tps < 256 && tps < n) tps *= 2;
+  while (tps < 256 && tps * 4 < n) tps *= 2;
   p.tps = tps;
+  const int rows = (n + tps - 1) / tps;
+  if (rows > kPTMaxRows) return TRIDI_ERROR_UNSUPPORTED_SIZE;
   p.G = 256 / tps > 0 ? 256 / tps : 1;
-  if ((long)p.G * n * 4 * sizeof(T) > 64 * 1024) p.G = 1;
+  while (p.G > 1 && (long)p.G * n * 4 * sizeof(T) > 64 * 1024) p.G /= 2;
   p.ct = p.G * tps;
-  if ((n + p.tps - 1) / p.tps > max_rows) return TRIDI_ERROR_UNSUPPORTED_SIZE;
   p.ntiles = (int)(((long)m + p.G - 1) / p.G);
   const bool tma_ok = aligned16(a) && aligned16(b) && aligned16(c) && aligned16(d) &&
                       ((size_t)n * sizeof(T)) % 16 == 0;
@@ -223,7 +236,11 @@ tridi_status pcr_thomas_device(const T* a, const T* b, const T* c, const T* d, T
   if (pt_smem<T>(S, p.G, n) > (size_t)dev->max_smem_optin) return TRIDI_ERROR_UNSUPPORTED_SIZE;
   p.stages = S;
   const size_t smem = pt_smem<T>(S, p.G, n);
-  auto kern = pcr_thomas_kernel<T, 288>;
+  auto kern = rows <= 1 ? pcr_thomas_kernel<T, 288, 1>
+              : rows <= 2 ? pcr_thomas_kernel<T, 288, 2>
+              : rows <= 4 ? pcr_thomas_kernel<T, 288, 4>
+              : rows <= 8 ? pcr_thomas_kernel<T, 288, 8>
+                          : pcr_thomas_kernel<T, 288, 16>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e);
   int per_sm = 0;

@@ -88,7 +88,8 @@ def crpcrNBC(a, b, c, d, rest_system_size, x=None, system_size=None):
 def pcrGauss(a, b, c, d, gaussian, x=None, system_size=None):
     """PCR-then-Thomas with `gaussian` interleaved subsystems (pcrGauss_app.cu:164),
     exact for every power-of-two gaussian; gaussian = 0 takes the autotuned
-    split for this size (else one Thomas chain per thread)."""
+    split for this size (else n/2 for power-of-two n: log2(n/2) PCR steps and
+    2-row chains, solved by the register PCR kernels)."""
     return _call("pcr_thomas", a, b, c, d, x, system_size, int(gaussian))
 
 
