@@ -1,7 +1,7 @@
 """Baseline timings for the benchmark spec (test infrastructure, not the product).
 
 Times, on the GPU machine:
-  * the reference's own FP32 kernels, rebuilt for sm_103a from its sources
+  * the reference's own FP32 kernels (pcrGauss rows: `rest` is g), rebuilt for sm_103a from its sources
     (oracle/_ref cubins, launched by oracle/ref_kernels_runner.cpp with the
     reference launchers' grid / block / shared sizes), beside this project's
     kernels on the same inputs;
@@ -45,6 +45,7 @@ def time_reference(kind, n, m, rest, reps):
     a, b, c, d = workloads.dominant(m, n, seed=workloads.SEEDS["c2"])
     src = [torch.from_numpy(v).cuda() for v in (a, b, c, d)]
     work = [torch.empty_like(t) for t in src]
+    ping = [torch.empty_like(t) for t in src] if kind == "pcrGauss" else None
     x = torch.empty_like(src[0])
     times = []
     for r in range(reps + 3):
@@ -52,7 +53,10 @@ def time_reference(kind, n, m, rest, reps):
             w.copy_(s)
         e0, e1 = _events()
         e0.record()
-        rk.solve(kind, *work, x, n, m, rest, torch.cuda.current_stream().cuda_stream)
+        if kind == "pcrGauss":  # rest = g; the solution is left in d or its ping buffer
+            rk.pcr_gauss(*work, *ping, n, m, rest, torch.cuda.current_stream().cuda_stream)
+        else:
+            rk.solve(kind, *work, x, n, m, rest, torch.cuda.current_stream().cuda_stream)
         e1.record()
         torch.cuda.synchronize()
         if r >= 3:
@@ -77,7 +81,8 @@ def time_ours(kind, n, m, rest, reps):
           "crpcr": lambda: L.tridi_crpcr_f32(*ptrs, n, m, rest, sp),
           "crNBC": lambda: L.tridi_cr_nbc_f32(*ptrs, n, m, sp),
           "crpcrNBC": lambda: L.tridi_crpcr_nbc_f32(*ptrs, n, m, rest, sp),
-          "crNBC32": lambda: L.tridi_cr_nbc_f32(*ptrs, n, m, sp)}[kind]
+          "crNBC32": lambda: L.tridi_cr_nbc_f32(*ptrs, n, m, sp),
+          "pcrGauss": lambda: L.tridi_pcr_thomas_f32(*ptrs, n, m, rest, sp)}[kind]
     times = []
     for r in range(reps + 3):
         e0, e1 = _events()
@@ -102,6 +107,8 @@ def gpu_rows(reps, peak):
             cases.append(("crpcr", n, m, rest))
             rest *= 2
         cases.append(("crpcrNBC", n, m, 32 if n >= 64 else 2))
+        if n <= 1024:  # the reference's small pcrGauss path; g = 8 (exact there) and n/2 (at most 512)
+            cases += [("pcrGauss", n, m, 8), ("pcrGauss", n, m, min(n // 2, 512))]
     for kind, n, m, rest in cases:
         row = {"kernel": kind, "n": n, "m": m, "rest": rest or None}
         for who, f in (("reference", time_reference), ("ours", time_ours)):

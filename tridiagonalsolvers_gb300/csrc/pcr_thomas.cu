@@ -148,22 +148,32 @@ __global__ void __launch_bounds__(MAXT) pcr_thomas_kernel(PTParams p) {
     }
 
     // ---- g independent Thomas chains of stride g (serial<T,g>) ----
+    // (the previous row's c' and d' carried in registers, so each step's
+    // dependent chain is arithmetic only; the row loads do not depend on it)
     for (int ch = t; ch < p.g; ch += tps) {
       const int gg = p.g;
-      wc[ch] = tdiv(wc[ch], wb[ch]);
-      wd[ch] = tdiv(wd[ch], wb[ch]);
+      T* __restrict__ cc = wc;
+      T* __restrict__ dd = wd;
+      const T* __restrict__ aa = wa;
+      const T* __restrict__ bb = wb;
+      T cprev = tdiv(cc[ch], bb[ch]);
+      T dprev = tdiv(dd[ch], bb[ch]);
+      cc[ch] = cprev;
+      dd[ch] = dprev;
       int last = ch;
       for (int i = ch + gg; i < n; i += gg) {
-        const T a = wa[i];
-        const T den = wb[i] - a * wc[i - gg];
-        wc[i] = tdiv(wc[i], den);
-        wd[i] = tdiv(wd[i] - wd[i - gg] * a, den);
+        const T a = aa[i];
+        const T den = bb[i] - a * cprev;
+        cprev = tdiv(cc[i], den);
+        dprev = tdiv(dd[i] - dprev * a, den);
+        cc[i] = cprev;
+        dd[i] = dprev;
         last = i;
       }
-      T xn = wd[last];
+      T xn = dprev;
       for (int i = last - gg; i >= 0; i -= gg) {
-        xn = wd[i] - wc[i] * xn;
-        wd[i] = xn;
+        xn = dd[i] - cc[i] * xn;
+        dd[i] = xn;
       }
     }
     consumer_sync(ct);
