@@ -415,6 +415,77 @@ __device__ __forceinline__ void hybrid_solve(Row<T> (&r)[K], T (&xr)[K], int t, 
       }
       const T xu = __shfl_up_sync(kFull, xC, 1, 32);
       x_prev = lane == 0 ? xpw : xu;
+    } else if (rest <= 32) {
+      // Block group, P < 32: the CR levels D < P stay inside each warp (as
+      // above, lane 31 redoes its chain from the next warp's exported rows);
+      // the rest <= 32 rows of the intermediate system are gathered into the
+      // group's first warp, which solves them by PCR on shuffles (normalised
+      // rows, end couplings zeroed, see pcr_regs_warp) and the closing 2x2
+      // systems, with no barrier in between; the back substitution is in
+      // each warp again.
+      const int lane = threadIdx.x & 31, wcta = threadIdx.x >> 5;
+      Row<T>* ex2 = exports + (ct / 32 + 1) * (LOGK > 0 ? LOGK : 1);
+      const Row<T> c0 = C;
+      Row<T> left[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int D = 1 << e;
+        if (D < P) {
+          left[e] = shfl_up(C, D, 32);
+          const Row<T> N = reduce_row(C, left[e], shfl_down(C, D, 32));
+          if (((lane + 1) & (2 * D - 1)) == 0) C = N;
+        }
+      }
+      if (lane < 16 && (lane & (lane + 1)) == 0 && lane + 1 < P) ex2[wcta * 5 + (31 - __clz(lane + 1))] = C;
+      consumer_sync(ct);
+      if (lane == 31 && !last_thread) {
+        Row<T> c = c0;
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if ((1 << e) < P) c = reduce_row(c, left[e], ex2[(wcta + 1) * 5 + e]);
+        C = c;
+      }
+      if (on) sc.put(j, C);
+      consumer_sync(ct);
+      if ((t >> 5) == 0) {  // the group's first warp: lane l holds intermediate row l
+        Row<T> y = lane < rest ? sc.get(lane) : Row<T>{T(0), T(1), T(0), T(0)};
+        if (lane == 0) y.a = T(0);
+        if (lane == rest - 1) y.c = T(0);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int dl = 1 << e;
+          if (4 * dl <= rest) {
+            const NRow<T> w = normalize_row(y);
+            y = reduce_row_nrm(y, shfl_up(w, dl, rest), shfl_down(w, dl, rest));
+          }
+        }
+        const bool upper = (lane & (rest - 1)) < rest / 2;
+        const NRow<T> w = normalize_row(y);
+        const T pd = __shfl_xor_sync(kFull, w.d, rest / 2, rest);
+        const T pk = __shfl_xor_sync(kFull, upper ? w.c : w.a, rest / 2, rest);
+        const T k = upper ? y.c : y.a;
+        const T xj = tdiv(y.d - k * pd, y.b - k * pk);
+        if (lane < rest) sc.x[lane] = xj;
+      }
+      consumer_sync(ct);
+      if (on) xC = sc.x[j];
+      // back substitution D = P/2..1 inside each warp; lane D-1's left
+      // neighbour is the previous warp's lane 31 (intermediate row
+      // 32 w / P - 1)
+      const int w0 = t - lane;  // the warp's first thread in the group
+      const T xpw = w0 > 0 ? sc.x[w0 / P - 1] : T(0);
+#pragma unroll
+      for (int e = 3; e >= 0; --e) {
+        const int D = 1 << e;
+        if (D < P) {
+          const T xu = __shfl_up_sync(kFull, xC, D, 32);
+          const T xrr = __shfl_down_sync(kFull, xC, D, 32);
+          const T v = back_row(C, lane < D ? xpw : xu, xrr, t == D - 1);
+          if (((lane + 1) & (2 * D - 1)) == D) xC = v;
+        }
+      }
+      const T xu = __shfl_up_sync(kFull, xC, 1, 32);
+      x_prev = lane == 0 ? xpw : xu;
     } else {
       sc.put(t, C);
       consumer_sync(ct);
