@@ -30,6 +30,8 @@
 //     release the stage, solve, and write x with 16-byte global stores.
 //     Inputs too small or misaligned for bulk copies are read directly.
 #pragma once
+#include <type_traits>
+
 #include "tridi_device.cuh"
 
 namespace tridi {
@@ -415,13 +417,13 @@ __device__ __forceinline__ void hybrid_solve(Row<T> (&r)[K], T (&xr)[K], int t, 
       }
       const T xu = __shfl_up_sync(kFull, xC, 1, 32);
       x_prev = lane == 0 ? xpw : xu;
-    } else if (rest <= 32) {
+    } else if (rest <= 64) {
       // Block group, P < 32: the CR levels D < P stay inside each warp (as
       // above, lane 31 redoes its chain from the next warp's exported rows);
-      // the rest <= 32 rows of the intermediate system are gathered into the
-      // group's first warp, which solves them by PCR on shuffles (normalised
-      // rows, end couplings zeroed, see pcr_regs_warp) and the closing 2x2
-      // systems, with no barrier in between; the back substitution is in
+      // the rest <= 64 rows of the intermediate system are gathered into the
+      // group's first warp (1 or 2 consecutive rows a lane), which solves
+      // them with pcr_regs_warp (PCR on shuffles and the closing 2x2
+      // systems), with no barrier in between; the back substitution is in
       // each warp again.
       const int lane = threadIdx.x & 31, wcta = threadIdx.x >> 5;
       Row<T>* ex2 = exports + (ct / 32 + 1) * (LOGK > 0 ? LOGK : 1);
@@ -447,25 +449,25 @@ __device__ __forceinline__ void hybrid_solve(Row<T> (&r)[K], T (&xr)[K], int t, 
       }
       if (on) sc.put(j, C);
       consumer_sync(ct);
-      if ((t >> 5) == 0) {  // the group's first warp: lane l holds intermediate row l
-        Row<T> y = lane < rest ? sc.get(lane) : Row<T>{T(0), T(1), T(0), T(0)};
-        if (lane == 0) y.a = T(0);
-        if (lane == rest - 1) y.c = T(0);
+      if ((t >> 5) == 0) {  // the group's first warp
+        const auto solve_gathered = [&](auto rows_tag) {
+          constexpr int RL = decltype(rows_tag)::value;  // intermediate rows a lane
+          const int lanes = rest / RL;                    // lanes holding them (a power of two <= 32)
+          Row<T> y[RL];
+          T xs[RL];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int dl = 1 << e;
-          if (4 * dl <= rest) {
-            const NRow<T> w = normalize_row(y);
-            y = reduce_row_nrm(y, shfl_up(w, dl, rest), shfl_down(w, dl, rest));
+          for (int q = 0; q < RL; ++q)
+            y[q] = lane < lanes ? sc.get(lane * RL + q) : Row<T>{T(0), T(1), T(0), T(0)};
+          pcr_regs_warp<T, RL, 1>(y, xs, lane & (lanes - 1), lanes);
+          if (lane < lanes) {
+#pragma unroll
+            for (int q = 0; q < RL; ++q) sc.x[lane * RL + q] = xs[q];
           }
-        }
-        const bool upper = (lane & (rest - 1)) < rest / 2;
-        const NRow<T> w = normalize_row(y);
-        const T pd = __shfl_xor_sync(kFull, w.d, rest / 2, rest);
-        const T pk = __shfl_xor_sync(kFull, upper ? w.c : w.a, rest / 2, rest);
-        const T k = upper ? y.c : y.a;
-        const T xj = tdiv(y.d - k * pd, y.b - k * pk);
-        if (lane < rest) sc.x[lane] = xj;
+        };
+        if (rest <= 32)
+          solve_gathered(std::integral_constant<int, 1>{});
+        else
+          solve_gathered(std::integral_constant<int, 2>{});
       }
       consumer_sync(ct);
       if (on) xC = sc.x[j];
