@@ -79,3 +79,49 @@ def test_refine_full_size_1024x65536_interleaved(cuda, residual):
     xs = x.view(n, m)[:, cols].cpu().numpy()
     _check(a[:, cols], b[:, cols], c[:, cols], d[:, cols], xs, 1, sweeps, rel)
     print(f"1024x65536 interleaved weak: {sweeps} sweeps to {rel:.2e}")
+
+
+@pytest.mark.parametrize("residual", ["df", "fp64"])
+@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("max_sweeps", [0, 1, 2, 3])
+def test_refine_every_sweep_count(cuda, residual, layout, max_sweeps):
+    """An unreachable tolerance runs exactly max_sweeps corrections and
+    reports non-convergence; x is still the refined solution of that many
+    sweeps (FP32-level after none, at the 1e-10 level after one or more) --
+    every path of the sweep sequence (first sweep only, the FP64 write of the
+    second, pairs again from the third) ends with x in FP64."""
+    import ctypes
+
+    import torch
+
+    from tridiagonalsolvers_gb300 import _lib
+
+    n, m = (1000, 17) if layout == 0 else (2048, 64)
+    a, b, c, d = workloads.dominant(m, n, seed=31 + max_sweeps, layout=layout)
+    t = _dev(cuda, a, b, c, d)
+    x = torch.full((n * m,), float("nan"), dtype=torch.float64, device=cuda)
+    L = _lib.lib()
+    wsb = L.tridi_refine_workspace_bytes(n, m, layout)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=cuda)
+    sweeps, rel = ctypes.c_int(-1), ctypes.c_double(0.0)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    prev = L.tridi_get_tunable(4)
+    L.tridi_set_tunable(4, {"df": 1, "fp64": 2}[residual])
+    try:
+        st = L.tridi_refine_f32(*(v.data_ptr() for v in t), x.data_ptr(), n, m, layout, 1e-30, max_sweeps,
+                                ws.data_ptr(), wsb, stream, ctypes.byref(sweeps), ctypes.byref(rel))
+    finally:
+        L.tridi_set_tunable(4, prev)
+    torch.cuda.synchronize()
+    assert st == 6 and sweeps.value == max_sweeps  # TRIDI_ERROR_NOT_CONVERGED after max_sweeps corrections
+    shp = (m, n) if layout == 0 else (n, m)
+    xs = x.cpu().numpy().reshape(shp)
+    assert np.all(np.isfinite(xs))
+    res = gold.rel_residual(a, b, c, d, xs, layout=layout)
+    if max_sweeps == 0:
+        assert res.max() <= 2e-6
+    else:
+        assert res.max() <= TOL, f"{max_sweeps} sweeps: oracle residual {res.max():.2e}"
+    # the kernel's own maximum agrees with the oracle's (both near the floor
+    # of the residual arithmetic after two or three sweeps)
+    assert rel.value <= 4 * res.max() + 1e-13 and res.max() <= 4 * rel.value + 1e-13

@@ -12,8 +12,10 @@
 // The update and the residual are one kernel; x is ping-ponged between two
 // 8-byte-per-row buffers so neighbours are read before they are rewritten.
 // Only those two steps run in extended precision: native FP64, or (the
-// default, TRIDI_TUNE_RESIDUAL) double-float, x held as (hi, lo) FP32 pairs
-// in the same buffers and assembled into FP64 once at the end.
+// default, TRIDI_TUNE_RESIDUAL) double-float, x held as (hi, lo) FP32 pairs.
+// In double-float x_1 = e_0 stays in FP32 and the second sweep writes
+// x_2 = e_0 + e_1 straight to FP64 (one correction: no pair buffer, no
+// assembly pass); further sweeps run on pairs, assembled into FP64 at the end.
 #include <algorithm>
 #include <cmath>
 
@@ -36,6 +38,9 @@ struct RefineParams {
   const float* e;     // FP32 correction
   const double* xin;  // x_k (ignored when first)
   double* xout;       // x_{k+1} (double-float mode: (hi, lo) FP32 pairs in the same 8 bytes)
+  const float* x1f;   // double-float mode 1: x_1 = e_0 in FP32
+  int mode;           // double-float mode: 0 first sweep (x_1 = e, not written), 1 second sweep
+                      // (x_2 = x1f + e, written as FP64), 2 later sweeps (pairs in, pairs out)
   float* r;           // FP32 copy of the residual
   double* rr;         // per-system sum of r^2 (accumulated)
   double* dd;         // per-system sum of d^2 (accumulated on the first sweep)
@@ -68,14 +73,21 @@ struct XNext<false> {
     return (float)r;
   }
 };
-template <>
-struct XNext<true> {
+// Double-float x; MODE (p.mode, a compile-time choice of the launch): 0
+// x = e, not written; 1 x = x1f + e, written in FP64; 2 pairs in, pairs out.
+template <int MODE>
+struct XDF {
   using V = float2;
   __device__ __forceinline__ static V get(const RefineParams& p, long k) {
-    return p.first ? make_float2(p.e[k], 0.f) : df_add(reinterpret_cast<const float2*>(p.xin)[k], p.e[k]);
+    if constexpr (MODE == 0) return make_float2(p.e[k], 0.f);
+    else if constexpr (MODE == 1) return df_add(make_float2(p.x1f[k], 0.f), p.e[k]);
+    else return df_add(reinterpret_cast<const float2*>(p.xin)[k], p.e[k]);
   }
   __device__ __forceinline__ static void put(const RefineParams& p, long k, V v) {
-    reinterpret_cast<float2*>(p.xout)[k] = v;
+    if constexpr (MODE == 1)
+      p.xout[k] = df_to_double(v.x, v.y);
+    else if constexpr (MODE == 2)
+      reinterpret_cast<float2*>(p.xout)[k] = v;
   }
   __device__ __forceinline__ static V zero() { return make_float2(0.f, 0.f); }
   __device__ __forceinline__ static float residual(const RefineParams& p, long i, long k, long stride, V xi,
@@ -86,6 +98,22 @@ struct XNext<true> {
     return df_residual(i > 0 ? p.a[k] : 0.f, p.b[k], i < p.n - 1 ? p.c[k] : 0.f, p.d[k], xm, xi, xp);
   }
 };
+
+// x = e exactly in FP64 (refinement that stops after its first sweep).
+__global__ void __launch_bounds__(256) refine_f32_to_fp64_kernel(const float* src, double* dst, long count) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x)
+    dst[k] = f2d_exact(src[k]);
+}
+
+// FP64 x split into normalised double-float pairs (a third sweep after the
+// second wrote x in FP64; rare): hi = x rounded to FP32, lo = the rest.
+__global__ void __launch_bounds__(256) refine_fp64_to_df_kernel(const double* src, float2* dst, long count) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
+    const double v = src[k];
+    const float hi = __double2float_rn(v);
+    dst[k] = make_float2(hi, __double2float_rn(v - (double)hi));
+  }
+}
 
 // The final double-float x assembled into FP64 (in place when src == dst:
 // each element is read before it is written, by the same thread).
@@ -99,9 +127,8 @@ __global__ void __launch_bounds__(256) refine_df_to_fp64_kernel(const float2* sr
 // Contiguous layout: block (system s, chunk q) covers rows [q*R, q*R + R).
 // Per-thread norm partial sums in FP32 (a few rows each), the block's sums
 // in FP64.
-template <bool DF>
+template <class X>
 __global__ void __launch_bounds__(256) refine_contig_kernel(RefineParams p) {
-  using X = XNext<DF>;
   const long chunks = (p.n + p.rows_per_block - 1) / p.rows_per_block;
   const long s = blockIdx.x / chunks, q = blockIdx.x % chunks;
   float rsf = 0.f, dsf = 0.f;
@@ -140,9 +167,8 @@ __global__ void __launch_bounds__(256) refine_contig_kernel(RefineParams p) {
 }
 
 // Interleaved layout: block = 32 systems x 8 row lanes, rows [q*R, q*R + R).
-template <bool DF>
+template <class X>
 __global__ void __launch_bounds__(256) refine_inter_kernel(RefineParams p) {
-  using X = XNext<DF>;
   const long groups = (p.m + 31) / 32;
   const long g = blockIdx.x % groups, q = blockIdx.x / groups;
   const long s = g * 32 + (threadIdx.x & 31);
@@ -204,10 +230,11 @@ namespace {
 
 long align64(long v) { return (v + 63) & ~63L; }
 
-// Workspace layout (bytes): e (4 nm), r (4 nm), xalt (8 nm), rr (8 m), dd (8 m),
-// scalar (8), then the large solver's workspace if needed.
+// Workspace layout (bytes): e (4 nm), e2 (4 nm), r (4 nm), xalt (8 nm), rr (8 m),
+// dd (8 m), scalar (8), then the large solver's workspace if needed.
 struct RefineWs {
   float* e;
+  float* e2;  // double-float mode: the first correction (e holds x_1 = e_0 meanwhile)
   float* r;
   double* xalt;
   double* rr;
@@ -228,7 +255,7 @@ size_t inner_bytes(long n, long m, int layout) {
 
 size_t refine_ws_bytes(long n, long m, int layout) {
   const long nm = align64(n * m);
-  return (size_t)nm * (4 + 4 + 8) + (size_t)align64(m) * 16 + 256 + inner_bytes(n, m, layout) + 1024;
+  return (size_t)nm * (4 + 4 + 4 + 8) + (size_t)align64(m) * 16 + 256 + inner_bytes(n, m, layout) + 1024;
 }
 
 RefineWs carve(void* ws, long n, long m, int layout) {
@@ -236,6 +263,7 @@ RefineWs carve(void* ws, long n, long m, int layout) {
   const long nm = align64(n * m);
   RefineWs r;
   r.e = reinterpret_cast<float*>(w); w += nm * 4;
+  r.e2 = reinterpret_cast<float*>(w); w += nm * 4;
   r.r = reinterpret_cast<float*>(w); w += nm * 4;
   r.xalt = reinterpret_cast<double*>(w); w += nm * 8;
   r.rr = reinterpret_cast<double*>(w); w += align64(m) * 8;
@@ -286,55 +314,107 @@ tridi_status refine_device(const float* a, const float* b, const float* c, const
   RefineParams p{};
   p.a = a; p.b = b; p.c = c; p.d = d; p.e = w.e; p.r = w.r; p.rr = w.rr; p.dd = w.dd;
   p.n = n; p.m = m; p.layout = layout;
-  // x_k alternates between the workspace copy and x; the first update
-  // writes the workspace, so one correction (the usual case) ends in x and
-  // the FP64 mode needs no final copy
-  double* bufs[2] = {x, w.xalt};
-  int cur = 0;  // x_k lives in bufs[cur]
   double rel = 0.0;
-  int sweep = 0;
-  for (;; ++sweep) {
-    p.first = sweep == 0;
-    p.xin = bufs[cur];
-    p.xout = bufs[cur ^ 1];
-    if ((e = cudaMemsetAsync(w.rr, 0, sizeof(double) * m, st)) != cudaSuccess) return cuda_status(e);
+  // One update + residual pass over the batch with the current p, then the
+  // maximum relative residual read back into rel.
+  const auto pass = [&]() -> cudaError_t {
+    cudaError_t ce;
+    if ((ce = cudaMemsetAsync(w.rr, 0, sizeof(double) * m, st)) != cudaSuccess) return ce;
     unsigned blocks;
     if (layout == 0) {
       p.rows_per_block = n < 2048 ? (int)n : 2048;
       const long chunks = (n + p.rows_per_block - 1) / p.rows_per_block;
       blocks = (unsigned)(m * chunks);
-      if (df)
-        refine_contig_kernel<true><<<blocks, 256, 0, st>>>(p);
+      if (!df)
+        refine_contig_kernel<XNext<false>><<<blocks, 256, 0, st>>>(p);
+      else if (p.mode == 0)
+        refine_contig_kernel<XDF<0>><<<blocks, 256, 0, st>>>(p);
+      else if (p.mode == 1)
+        refine_contig_kernel<XDF<1>><<<blocks, 256, 0, st>>>(p);
       else
-        refine_contig_kernel<false><<<blocks, 256, 0, st>>>(p);
+        refine_contig_kernel<XDF<2>><<<blocks, 256, 0, st>>>(p);
     } else {
       p.rows_per_block = 256;
       const long groups = (m + 31) / 32, chunks = (n + 255) / 256;
       blocks = (unsigned)(groups * chunks);
-      if (df)
-        refine_inter_kernel<true><<<blocks, 256, 0, st>>>(p);
+      if (!df)
+        refine_inter_kernel<XNext<false>><<<blocks, 256, 0, st>>>(p);
+      else if (p.mode == 0)
+        refine_inter_kernel<XDF<0>><<<blocks, 256, 0, st>>>(p);
+      else if (p.mode == 1)
+        refine_inter_kernel<XDF<1>><<<blocks, 256, 0, st>>>(p);
       else
-        refine_inter_kernel<false><<<blocks, 256, 0, st>>>(p);
+        refine_inter_kernel<XDF<2>><<<blocks, 256, 0, st>>>(p);
     }
-    cur = (p.xout == x) ? 0 : 1;
     refine_maxrel_kernel<<<1, 1024, 0, st>>>(w.rr, w.dd, m, w.scalar);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
-    if ((e = cudaMemcpyAsync(&rel, w.scalar, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+    if ((ce = cudaGetLastError()) != cudaSuccess) return ce;
+    if ((ce = cudaMemcpyAsync(&rel, w.scalar, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return ce;
+    return cudaStreamSynchronize(st);
+  };
+  const auto done = [&](int sw) { return rel <= tol || sw >= max_sweeps || !(rel == rel); };
+  const long count = n * m;
+  const unsigned eblocks = (unsigned)std::min<long>((count + 255) / 256, 65535L * 8);
+  int sweep = 0;
+  if (df) {
+    // Double-float.  Sweep 0: x_1 = e_0 stays in w.e (FP32, exact), only r_1
+    // is written.  Sweep 1: x_2 = e_0 + e_1 (an exact pair) goes to x in FP64
+    // directly, so one correction (the usual case) needs no pair buffer and
+    // no assembly pass.  Later sweeps (rare) split x into pairs again and run
+    // on pairs, assembled into FP64 at the end.
+    p.first = 1;
+    p.mode = 0;
+    if ((e = pass()) != cudaSuccess) return cuda_status(e);
+    if (done(0)) {
+      refine_f32_to_fp64_kernel<<<eblocks, 256, 0, st>>>(w.e, x, count);
+      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+    } else {
+      sweep = 1;
+      if ((ts = solve32(a, b, c, w.r, w.e2, n, m, layout, w, stream)) != TRIDI_SUCCESS) return ts;
+      p.first = 0;
+      p.mode = 1;
+      p.x1f = w.e;
+      p.e = w.e2;
+      p.xout = x;
+      if ((e = pass()) != cudaSuccess) return cuda_status(e);
+      if (!done(1)) {
+        refine_fp64_to_df_kernel<<<eblocks, 256, 0, st>>>(x, reinterpret_cast<float2*>(w.xalt), count);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+        // x_k alternates between the workspace copy and x (neighbours are
+        // read before they are rewritten)
+        double* bufs[2] = {x, w.xalt};
+        int cur = 1;
+        p.mode = 2;
+        p.e = w.e;
+        for (sweep = 2;; ++sweep) {
+          if ((ts = solve32(a, b, c, w.r, w.e, n, m, layout, w, stream)) != TRIDI_SUCCESS) return ts;
+          p.xin = bufs[cur];
+          p.xout = bufs[cur ^ 1];
+          if ((e = pass()) != cudaSuccess) return cuda_status(e);
+          cur ^= 1;
+          if (done(sweep)) break;
+        }
+        // x_k as double-float pairs in bufs[cur] -> FP64 in x
+        refine_df_to_fp64_kernel<<<eblocks, 256, 0, st>>>(reinterpret_cast<const float2*>(bufs[cur]), x, count);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+      }
+    }
+  } else {
+    // Native FP64: x_k alternates between the workspace copy and x; the first
+    // update writes the workspace, so one correction ends in x.
+    double* bufs[2] = {x, w.xalt};
+    int cur = 0;  // x_k lives in bufs[cur]
+    for (;; ++sweep) {
+      p.first = sweep == 0;
+      p.xin = bufs[cur];
+      p.xout = bufs[cur ^ 1];
+      if ((e = pass()) != cudaSuccess) return cuda_status(e);
+      cur = (p.xout == x) ? 0 : 1;
+      if (done(sweep)) break;
+      if ((ts = solve32(a, b, c, w.r, w.e, n, m, layout, w, stream)) != TRIDI_SUCCESS) return ts;
+    }
+    if (cur != 0 &&
+        (e = cudaMemcpyAsync(x, bufs[cur], sizeof(double) * n * m, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
       return cuda_status(e);
-    if (rel <= tol || sweep >= max_sweeps || !(rel == rel)) break;
-    ts = solve32(a, b, c, w.r, w.e, n, m, layout, w, stream);
-    if (ts != TRIDI_SUCCESS) return ts;
-  }
-  if (df) {  // x_k as double-float pairs in bufs[cur] -> FP64 in x
-    const long count = n * m;
-    const unsigned blocks = (unsigned)std::min<long>((count + 255) / 256, 65535L * 8);
-    refine_df_to_fp64_kernel<<<blocks, 256, 0, st>>>(reinterpret_cast<const float2*>(bufs[cur]), x, count);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
-  } else if (cur != 0 &&
-             (e = cudaMemcpyAsync(x, bufs[cur], sizeof(double) * n * m, cudaMemcpyDeviceToDevice, st)) !=
-                 cudaSuccess) {
-    return cuda_status(e);
   }
   if (sweeps_out) *sweeps_out = sweep;
   if (res_out) *res_out = rel;
