@@ -84,18 +84,26 @@ def test_large_batch_65536x256(cuda):
     assert np.all(np.isfinite(x))
 
 
-def test_misaligned_pointers_take_the_direct_path(cuda):
+@pytest.mark.parametrize("n,rest", [(64, None), (1024, None), (1024, 4), (1024, 32), (2048, 64), (1024, 512)])
+def test_misaligned_pointers_take_the_direct_path(cuda, n, rest):
+    """Inputs 4 bytes off a 16-byte boundary go through the producer-warp
+    kernel without bulk copies: warp shapes, and the block shapes' CR levels
+    inside warps, gathered intermediate systems and shared-memory PCR."""
     import torch
 
-    n, m = 64, 10
-    a, b, c, d = workloads.dominant(m, n, seed=5)
+    m = 10
+    a, b, c, d = workloads.dominant(m, n, seed=5 + n)
     bufs = [torch.zeros(m * n + 1, dtype=torch.float32, device=cuda) for _ in range(5)]
     views = [t[1:] for t in bufs]  # 4-byte offset: not 16-byte aligned
     for v, h in zip(views[:4], (a, b, c, d)):
         v.copy_(torch.from_numpy(h.ravel()))
-    tg.cr(*views[:4], x=views[4], system_size=n)
+    if rest is None:
+        tg.cr(*views[:4], x=views[4], system_size=n)
+    else:
+        tg.crpcr(*views[:4], rest, x=views[4], system_size=n)
     x = views[4].view(m, n).cpu().numpy()
     check_against_oracle(a, b, c, d, x)
+    assert tg.device_status() == 0
 
 
 # ---- against the reference's own kernels -------------------------------------
