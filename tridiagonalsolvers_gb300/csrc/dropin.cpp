@@ -1,9 +1,12 @@
 // The reference's host launchers (include/tridi_dropin.h) on the GB300
 // kernels.  Host pointers in, host pointers out, synchronous.
 //
-// Per call: the batch is cut into chunks of whole systems; chunk i is copied
-// host->device, solved and copied back on stream i % 2, so the copies of one
-// chunk overlap the solve of another and host->device overlaps device->host.
+// Per call: the batch is cut into chunks of whole systems; every chunk's
+// host->device copies go back to back on a copy-in stream, its solve on a
+// compute stream after an event of its copies, its device->host copy on a
+// copy-out stream after an event of its solve.  So the host->device engine
+// (the bound: about 4/5 of the bytes) never waits behind a device->host copy,
+// and the copies of one chunk overlap the solve of another.
 // Device buffers come from a persistent per-device workspace (grown on
 // demand, never shrunk until tridi_dropin_release), not from a cudaMalloc
 // and cudaFree per call as in cr_app.cu:20-24,61-65.
@@ -29,10 +32,13 @@ tridi_status dropin_device_solve(int algo, const T* a, const T* b, const T* c, c
 
 namespace {
 
+constexpr int kMaxChunks = 64;
 struct Workspace {
   void* ptr = nullptr;
   size_t bytes = 0;
-  cudaStream_t stream[2] = {nullptr, nullptr};
+  cudaStream_t stream[3] = {nullptr, nullptr, nullptr};  // copy-in, compute, copy-out
+  cudaEvent_t in_done[kMaxChunks] = {};
+  cudaEvent_t solved[kMaxChunks] = {};
 };
 constexpr int kMaxDev = 64;
 Workspace g_ws[kMaxDev];
@@ -43,11 +49,14 @@ cudaError_t ensure_workspace(Workspace& w, size_t bytes) {
   if (!w.stream[0]) {
     for (auto& s : w.stream)
       if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) return e;
+    for (int k = 0; k < kMaxChunks; ++k) {
+      if ((e = cudaEventCreateWithFlags(&w.in_done[k], cudaEventDisableTiming)) != cudaSuccess) return e;
+      if ((e = cudaEventCreateWithFlags(&w.solved[k], cudaEventDisableTiming)) != cudaSuccess) return e;
+    }
   }
   if (w.bytes >= bytes) return cudaSuccess;
   if (w.ptr) {
-    cudaStreamSynchronize(w.stream[0]);
-    cudaStreamSynchronize(w.stream[1]);
+    for (auto& s : w.stream) cudaStreamSynchronize(s);
     cudaFree(w.ptr);
     w.ptr = nullptr;
     w.bytes = 0;
@@ -80,7 +89,7 @@ tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d
   const size_t chunk_bytes = chunk_kib > 0 ? (size_t)chunk_kib << 10 : (size_t)8 << 20;
   long per = (long)(chunk_bytes / sys_bytes);
   if (per < 1) per = 1;
-  if (per * 64 < m) per = (m + 63) / 64;
+  if (per * kMaxChunks < m) per = (m + kMaxChunks - 1) / kMaxChunks;
   if (per > m) per = m;
   const size_t arr = align256((size_t)m * sys_bytes);
   // chunks use disjoint slices of the scratch, each sized for a full chunk
@@ -96,29 +105,33 @@ tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d
   void* ws = base + 5 * arr;
 
   tridi_status st = TRIDI_SUCCESS;
+  cudaStream_t s_in = w.stream[0], s_comp = w.stream[1], s_out = w.stream[2];
   for (long s0 = 0, k = 0; s0 < m; s0 += per, ++k) {
     const long cnt = (m - s0) < per ? (m - s0) : per;
     const size_t off = (size_t)s0 * n, bytes = (size_t)cnt * sys_bytes;
-    cudaStream_t s = w.stream[k & 1];
-    if ((e = cudaMemcpyAsync(da + off, a + off, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(db + off, b + off, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(dc + off, c + off, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(dd + off, d + off, bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess) {
+    if ((e = cudaMemcpyAsync(da + off, a + off, bytes, cudaMemcpyHostToDevice, s_in)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(db + off, b + off, bytes, cudaMemcpyHostToDevice, s_in)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dc + off, c + off, bytes, cudaMemcpyHostToDevice, s_in)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(dd + off, d + off, bytes, cudaMemcpyHostToDevice, s_in)) != cudaSuccess ||
+        (e = cudaEventRecord(w.in_done[k], s_in)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(s_comp, w.in_done[k], 0)) != cudaSuccess) {
       st = cuda_status(e);
       break;
     }
     st = dropin_device_solve<T>(algo, da + off, db + off, dc + off, dd + off, dx + off, n, (int)cnt, param,
-                                static_cast<char*>(ws) + (size_t)k * ws_share, ws_share, s);
+                                static_cast<char*>(ws) + (size_t)k * ws_share, ws_share, s_comp);
     if (st != TRIDI_SUCCESS) break;
-    if ((e = cudaMemcpyAsync(x + off, dx + off, bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
+    if ((e = cudaEventRecord(w.solved[k], s_comp)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(s_out, w.solved[k], 0)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(x + off, dx + off, bytes, cudaMemcpyDeviceToHost, s_out)) != cudaSuccess) {
       st = cuda_status(e);
       break;
     }
   }
-  cudaError_t e0 = cudaStreamSynchronize(w.stream[0]);
-  cudaError_t e1 = cudaStreamSynchronize(w.stream[1]);
-  if (st == TRIDI_SUCCESS && (e0 != cudaSuccess || e1 != cudaSuccess))
-    st = cuda_status(e0 != cudaSuccess ? e0 : e1);
+  cudaError_t es[3];
+  for (int q = 0; q < 3; ++q) es[q] = cudaStreamSynchronize(w.stream[q]);
+  for (int q = 0; q < 3 && st == TRIDI_SUCCESS; ++q)
+    if (es[q] != cudaSuccess) st = cuda_status(es[q]);
   return st;
 }
 
@@ -247,6 +260,11 @@ tridi_status tridi_dropin_release(void) {
       cudaStreamDestroy(s);
       s = nullptr;
     }
+  for (int k = 0; k < tridi::kMaxChunks; ++k) {
+    if (w.in_done[k]) cudaEventDestroy(w.in_done[k]);
+    if (w.solved[k]) cudaEventDestroy(w.solved[k]);
+    w.in_done[k] = w.solved[k] = nullptr;
+  }
   if (w.ptr) cudaFree(w.ptr);
   w.ptr = nullptr;
   w.bytes = 0;
