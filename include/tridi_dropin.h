@@ -28,7 +28,14 @@
  * What changed underneath: no cudaMalloc/cudaFree per call (a persistent
  * device workspace that grows on demand, guarded by a mutex), and the batch is
  * split into chunks whose host->device copy, solve and device->host copy
- * overlap on two streams.  The solver kernels themselves are in tridi.h.
+ * overlap on three streams.  The solver kernels themselves are in tridi.h.
+ *
+ * pcrGaussWrapper takes any systemSize >= 1, as the reference's does (its
+ * large path, pcrGauss_app.cu:196-228, takes every size above MINSYSTEM =
+ * 1024): PCR-then-Thomas with `gaussian` chains up to 4096 rows, the one-pass
+ * partition solver up to 8704 rows (FP32) / 4608 (FP64), the large-system
+ * solver beyond (its workspace is part of the persistent one).  Every path
+ * is exact; above 4096 rows `gaussian` does not change the result.
  *
  * The extern "C" functions below are the same launchers for foreign-function
  * callers (ctypes, cgo, JNI): status codes instead of exiting.

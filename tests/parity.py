@@ -23,14 +23,18 @@ FWD_TOL = {np.float32: 2e-5, np.float64: 1e-12}
 ULP_TOL = 64
 
 
-def check_against_oracle(a, b, c, d, x, layout=0, dtype=np.float32, res_tol=None, fwd_tol=None):
-    """a..d, x are host numpy arrays; returns (max residual, max fwd error)."""
+def check_against_oracle(a, b, c, d, x, layout=0, dtype=np.float32, res_tol=None, fwd_tol=None, x64=None):
+    """a..d, x are host numpy arrays; returns (max residual, max fwd error).
+    Every system is checked.  x64: the oracle's FP64 solution of these FP32
+    inputs when the caller already has it (several solvers checked against
+    one batch), else computed here."""
     a32, b32, c32, d32 = (np.asarray(v, np.float32) for v in (a, b, c, d))
     if dtype == np.float64:
         # FP64 inputs: residual and oracle computed from FP64 data directly.
         res, fwd = _f64_metrics(a, b, c, d, x, layout)
     else:
-        x64 = gold.solve_f64(a32, b32, c32, d32, layout=layout)
+        if x64 is None:
+            x64 = gold.solve_f64(a32, b32, c32, d32, layout=layout)
         res = gold.rel_residual(a32, b32, c32, d32, np.asarray(x), layout=layout)
         ax = 1 if layout == 0 else 0
         err = np.abs(np.asarray(x, np.float64) - x64).max(axis=ax)
@@ -92,7 +96,10 @@ def check_ulps_where_reference_valid(x, x_ref, a, b, c, d, dtype=np.float32, ulp
 
 
 def legacy_accept(x, a, b, c, d):
-    """The reference driver's own acceptance: RMS vs gold <= 1e-3 for every system."""
-    x_gold = gold.serial_many(*(np.asarray(v, np.float32) for v in (a, b, c, d)))
-    nf, _ = gold.compare_many(np.asarray(x, np.float32), x_gold, 1e-3)
+    """The reference driver's own acceptance: RMS vs gold <= 1e-3 for every
+    system, with the gold solver and the comparison in the inputs' precision
+    (float, or double in the reference's USE_DOUBLE build)."""
+    dt = np.float64 if np.asarray(a).dtype == np.float64 else np.float32
+    x_gold = gold.serial_many(*(np.asarray(v, dt) for v in (a, b, c, d)))
+    nf, _ = gold.compare_many(np.asarray(x, dt), x_gold, 1e-3)
     assert nf == 0, f"{nf} systems fail the reference's 1e-3 RMS acceptance"

@@ -102,3 +102,49 @@ def test_reference_large_pcr_gauss_path_is_approximate(cuda):
     res_ref = gold.rel_residual(a, b, c, d, xr).max()
     res_new = gold.rel_residual(a, b, c, d, x).max()
     assert res_new <= max(res_ref, 2e-6)
+
+
+# pcrGaussWrapper at every size the reference's large path accepts: the
+# reference takes any systemSize > MINSYSTEM = 1024 down its global-memory PCR
+# path (pcrGauss_app.cu:196-228, :102-162); its driver calls it at 2 x 8192
+# (test_tridiagonal.cpp:30-31,81).  Here: PCR-then-Thomas up to 4096 rows, the
+# partition solver up to 8704 (FP32) / 4608 (FP64) rows, the large-system
+# solver beyond, through the host-pointer drop-in.
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("n,m", [(8192, 2), (16384, 4), (65536, 2), (10007, 3), (5000, 3), (80000, 1)])
+def test_pcr_gauss_wrapper_large_sizes(cuda, prec, n, m):
+    dt = NP[prec]
+    if n == 8192:
+        a, b, c, d = gold.generate_reference_inputs(n, m, dt, seed=1)
+    else:
+        a, b, c, d = workloads.dominant(m, n, seed=40 + n + m, dtype=dt)
+    keep = [v.copy() for v in (a, b, c, d)]
+    x = np.zeros_like(a)
+    dropin.pcrGaussWrapper(a, b, c, d, x, n, m, 64)
+    for u, v in zip((a, b, c, d), keep):
+        assert np.array_equal(u, v)
+    check_against_oracle(a, b, c, d, x, dtype=dt)
+    legacy_accept(x, a, b, c, d)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_pcr_gauss_wrapper_large_weakly_dominant(cuda, prec):
+    dt = NP[prec]
+    n, m = 32768, 3
+    a, b, c, d = workloads.weak(m, n, seed=12, dtype=dt)
+    x = np.zeros_like(a)
+    dropin.pcrGaussWrapper(a, b, c, d, x, n, m, 64)
+    if prec == "f32":
+        check_against_oracle(a, b, c, d, x, res_tol=1e-5, fwd_tol=5e-3)
+    else:
+        check_against_oracle(a, b, c, d, x, dtype=dt, res_tol=1e-13, fwd_tol=1e-10)
+
+
+def test_pcr_gauss_wrapper_large_many_chunks(cuda):
+    """Enough 16384-row systems for several pipelined chunks sharing one
+    scratch slice of the large solver's workspace."""
+    n, m = 16384, 300
+    a, b, c, d = workloads.dominant(m, n, seed=77)
+    x = np.zeros_like(a)
+    dropin.pcrGaussWrapper(a, b, c, d, x, n, m, 64)
+    check_against_oracle(a, b, c, d, x)

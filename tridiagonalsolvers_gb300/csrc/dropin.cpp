@@ -33,6 +33,7 @@ tridi_status dropin_device_solve(int algo, const T* a, const T* b, const T* c, c
 namespace {
 
 constexpr int kMaxChunks = 64;
+constexpr int kTimedLaunches = 50;  // the reference's numIterations (common.h:14)
 struct Workspace {
   void* ptr = nullptr;
   size_t bytes = 0;
@@ -72,8 +73,13 @@ size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 template <class T>
 size_t algo_scratch(int algo, int n, int m, int param);
 
+// Stages the batch through the chunk pipeline.  The chunks' solves are
+// ordered on the one compute stream, so they share one scratch slice, sized
+// for a full chunk -- or for the whole batch when `whole_batch_scratch` is
+// set (the timing path relaunches the device work on all m systems at once).
 template <class T>
-tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d, T* x, int n, int m, int param) {
+tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d, T* x, int n, int m, int param,
+                        bool whole_batch_scratch = false) {
   if (!a || !b || !c || !d || !x || n <= 0 || m <= 0) return TRIDI_ERROR_INVALID_VALUE;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -92,10 +98,12 @@ tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d
   if (per * kMaxChunks < m) per = (m + kMaxChunks - 1) / kMaxChunks;
   if (per > m) per = m;
   const size_t arr = align256((size_t)m * sys_bytes);
-  // chunks use disjoint slices of the scratch, each sized for a full chunk
-  const long nchunks = (m + per - 1) / per;
-  const size_t ws_share = align256(algo_scratch<T>(algo, n, (int)per, param));
-  if ((e = ensure_workspace(w, 5 * arr + (size_t)nchunks * ws_share)) != cudaSuccess) return cuda_status(e);
+  size_t ws_bytes = align256(algo_scratch<T>(algo, n, (int)per, param));
+  if (whole_batch_scratch) {
+    const size_t whole = align256(algo_scratch<T>(algo, n, m, param));
+    if (whole > ws_bytes) ws_bytes = whole;
+  }
+  if ((e = ensure_workspace(w, 5 * arr + ws_bytes)) != cudaSuccess) return cuda_status(e);
   char* base = static_cast<char*>(w.ptr);
   T* da = reinterpret_cast<T*>(base);
   T* db = reinterpret_cast<T*>(base + arr);
@@ -118,8 +126,8 @@ tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d
       st = cuda_status(e);
       break;
     }
-    st = dropin_device_solve<T>(algo, da + off, db + off, dc + off, dd + off, dx + off, n, (int)cnt, param,
-                                static_cast<char*>(ws) + (size_t)k * ws_share, ws_share, s_comp);
+    st = dropin_device_solve<T>(algo, da + off, db + off, dc + off, dd + off, dx + off, n, (int)cnt, param, ws,
+                                ws_bytes, s_comp);
     if (st != TRIDI_SUCCESS) break;
     if ((e = cudaEventRecord(w.solved[k], s_comp)) != cudaSuccess ||
         (e = cudaStreamWaitEvent(s_out, w.solved[k], 0)) != cudaSuccess ||
@@ -140,37 +148,66 @@ const char* algo_name(int algo) {
   return algo >= 0 && algo < 7 ? names[algo] : "?";
 }
 
+// numIterations (common.h:14) = 50 timed launches of the device work on the
+// staged batch, printed like cr_app.cu:48 / pcrGauss_app.cu.  Runs after a
+// full host_solve that staged the inputs into the workspace, on the compute
+// stream, with CUDA events; every launch's status is checked.
+template <class T>
+tridi_status time_device_work(int algo, int n, int m, int param, float* ms_per_launch) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e);
+  std::lock_guard<std::mutex> lock(g_mu);
+  Workspace& w = g_ws[dev];
+  const size_t arr = align256((size_t)m * n * sizeof(T));
+  const size_t need = align256(algo_scratch<T>(algo, n, m, param));
+  if (!w.ptr || w.bytes < 5 * arr + need) return TRIDI_ERROR_WORKSPACE_TOO_SMALL;
+  char* base = static_cast<char*>(w.ptr);
+  cudaStream_t s = w.stream[1];
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  tridi_status st = TRIDI_SUCCESS;
+  if ((e = cudaEventCreate(&ev[0])) != cudaSuccess || (e = cudaEventCreate(&ev[1])) != cudaSuccess ||
+      (e = cudaEventRecord(ev[0], s)) != cudaSuccess)
+    st = cuda_status(e);
+  for (int i = 0; i < kTimedLaunches && st == TRIDI_SUCCESS; ++i)
+    st = dropin_device_solve<T>(algo, reinterpret_cast<T*>(base), reinterpret_cast<T*>(base + arr),
+                                reinterpret_cast<T*>(base + 2 * arr), reinterpret_cast<T*>(base + 3 * arr),
+                                reinterpret_cast<T*>(base + 4 * arr), n, m, param, base + 5 * arr,
+                                w.bytes - 5 * arr, s);
+  if (st == TRIDI_SUCCESS && (e = cudaEventRecord(ev[1], s)) != cudaSuccess) st = cuda_status(e);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess && st == TRIDI_SUCCESS) st = cuda_status(e);
+  if (st == TRIDI_SUCCESS) {
+    float ms = 0.f;
+    if ((e = cudaEventElapsedTime(&ms, ev[0], ev[1])) != cudaSuccess) st = cuda_status(e);
+    *ms_per_launch = ms / kTimedLaunches;
+  }
+  for (auto& v : ev)
+    if (v) cudaEventDestroy(v);
+  return st;
+}
+
 // The C++ drop-ins: reference error behaviour (print, then exit like
-// CUDA_SAFE_CALL) and the optional reference timing line.
+// CUDA_SAFE_CALL, unless TRIDI_DROPIN_NO_EXIT=1) and, with
+// TRIDI_DROPIN_TIMING=1, the reference's timing line.
 template <class T>
 void dropin(int algo, T* a, T* b, T* c, T* d, T* x, int n, int m, int param) {
   const char* timing = std::getenv("TRIDI_DROPIN_TIMING");
+  tridi_status st = TRIDI_SUCCESS;
   if (timing && timing[0] == '1') {
-    // numIterations (common.h:14) timed launches of the device work alone,
-    // printed like cr_app.cu:48: "<name>: numSystems: .., systemSize: .., GPU kernel time: .. ms".
-    host_solve<T>(algo, a, b, c, d, x, n, m, param);  // stage inputs + warm up
-    std::lock_guard<std::mutex> lock(g_mu);
-    int dev = 0;
-    cudaGetDevice(&dev);
-    Workspace& w = g_ws[dev];
-    const size_t arr = align256((size_t)m * n * sizeof(T));
-    char* base = static_cast<char*>(w.ptr);
-    const size_t scratch = w.bytes - 5 * arr;
-    cudaStreamSynchronize(w.stream[0]);
-    auto t0 = std::chrono::steady_clock::now();
-    for (int i = 0; i < 50; ++i)
-      dropin_device_solve<T>(algo, reinterpret_cast<T*>(base), reinterpret_cast<T*>(base + arr),
-                             reinterpret_cast<T*>(base + 2 * arr), reinterpret_cast<T*>(base + 3 * arr),
-                             reinterpret_cast<T*>(base + 4 * arr), n, m, param, base + 5 * arr, scratch,
-                             w.stream[0]);
-    cudaStreamSynchronize(w.stream[0]);
-    double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (algo == TRIDI_DROPIN_PCR_THOMAS)
-      printf("pcrGauss: GPU kernel time: %f ms\n", ms / 50);
-    else
-      printf("%s: numSystems: %d, systemSize: %d, GPU kernel time: %f ms\n", algo_name(algo), m, n, ms / 50);
+    float ms = 0.f;
+    st = host_solve<T>(algo, a, b, c, d, x, n, m, param, /*whole_batch_scratch=*/true);
+    if (st == TRIDI_SUCCESS) st = time_device_work<T>(algo, n, m, param, &ms);
+    if (st == TRIDI_SUCCESS) {
+      if (algo == TRIDI_DROPIN_PCR_THOMAS)
+        printf("pcrGauss: GPU kernel time: %f ms\n", ms);
+      else
+        printf("%s: numSystems: %d, systemSize: %d, GPU kernel time: %f ms\n", algo_name(algo), m, n, ms);
+      fflush(stdout);
+    }
   }
-  tridi_status st = host_solve<T>(algo, a, b, c, d, x, n, m, param);
+  // the solve whose x the caller gets (as the reference re-runs its kernel on
+  // fresh inputs after timing, cr_app.cu:50-56)
+  if (st == TRIDI_SUCCESS) st = host_solve<T>(algo, a, b, c, d, x, n, m, param);
   if (st != TRIDI_SUCCESS) {
     fprintf(stderr, "tridi: %s(systemSize=%d, numSystems=%d) failed: %s (cuda error %d)\n", algo_name(algo), n, m,
             tridi_status_string(st), tridi_last_cuda_error());

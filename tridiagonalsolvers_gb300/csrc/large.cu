@@ -10,7 +10,8 @@
 //   2. large_assemble: separator row j of system s from chunk j's interface
 //      and chunk j+1's first interior row, in the layout of the data.  The
 //      P = ceil(n/L) separators per system form a batch of the same kind,
-//      solved by the uniform partition solver (contiguous, P <= 8704) or by
+//      solved by the uniform partition solver (contiguous, P <= 8704 in FP32,
+//      4608 in FP64) or by
 //      this scheme again (interleaved, or larger P), down to a one-thread-
 //      per-system Thomas kernel for interleaved batches of <= 32 rows.
 //   3. large_back: each chunk is read and eliminated again and its rows
@@ -180,10 +181,17 @@ size_t large_ws_bytes(long n, long m, int layout) {
   if (layout == 1 && n <= kThomasMax) return (size_t)2 * round64(n * m) * sizeof(T) + 256;
   const long P = (n + kChunk - 1) / kChunk;
   size_t own = (size_t)14 * round64(P * m) * sizeof(T) + 256;
-  if (layout == 1 || P > 8704) own += large_ws_bytes<T>(P, m, layout);
+  if (layout == 1 || P > partition_max_rows<T>()) own += large_ws_bytes<T>(P, m, layout);
   return own;
 }
 }  // namespace
+
+template <class T>
+size_t large_workspace_bytes(long n, long m, int layout) {
+  return large_ws_bytes<T>(n, m, layout);
+}
+template size_t large_workspace_bytes<float>(long, long, int);
+template size_t large_workspace_bytes<double>(long, long, int);
 
 template <class T>
 tridi_status large_solve_device(const T* a, const T* b, const T* c, const T* d, T* x, long n, long m, int layout,
@@ -232,7 +240,7 @@ tridi_status large_solve_device(const T* a, const T* b, const T* c, const T* d, 
   if (e != cudaSuccess) return cuda_status(e);
   const T* r = static_cast<const T*>(p.red);
   tridi_status ts;
-  if (layout == 0 && p.P <= 8704 / (sizeof(T) == 4 ? 1 : 2))
+  if (layout == 0 && p.P <= partition_max_rows<T>())
     ts = partition_solve_device<T>(r, r + p.PMp, r + 2 * p.PMp, r + 3 * p.PMp, static_cast<T*>(p.sol), (int)p.P,
                                    (int)m, stream);
   else

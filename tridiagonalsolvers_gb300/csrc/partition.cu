@@ -190,7 +190,8 @@ tridi_status partition_solve_device(const T* a, const T* b, const T* c, const T*
   constexpr int kWarpMax = F32 ? 31 : 15;  // rows per lane in warp mode
   constexpr int kCtaMax = F32 ? 17 : 9;    // rows per thread in CTA mode (512 threads)
   if (!a || !b || !c || !d || !x || m <= 0) return TRIDI_ERROR_INVALID_VALUE;
-  if (n < 1 || n > 512 * kCtaMax) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  static_assert(512L * kCtaMax == partition_max_rows<T>(), "partition size cap");
+  if (n < 1 || n > partition_max_rows<T>()) return TRIDI_ERROR_UNSUPPORTED_SIZE;
   const DeviceInfo* dev = current_device();
   if (!dev) return TRIDI_ERROR_CUDA;
   PartParams p{};

@@ -52,6 +52,13 @@ inline int ilog2(long v) {
 // reduced until the shared memory fits the device.
 int pick_stages(size_t fixed_bytes, size_t stage_bytes, int fallback, const DeviceInfo& dev);
 
+// Largest system the uniform partition solver (tridi_solve_*) takes: 512
+// threads of 17 rows (FP32) or 9 rows (FP64) each.
+template <class T>
+constexpr long partition_max_rows() {
+  return sizeof(T) == 4 ? 512L * 17 : 512L * 9;
+}
+
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 inline bool is_pow2(long v) { return v > 0 && (v & (v - 1)) == 0; }
 
