@@ -289,6 +289,17 @@ tridi_status tridi_refine_f32(const float *a, const float *b, const float *c, co
 tridi_status tridi_selfcheck_df_to_double(const float *hi, const float *lo, double *out, long n,
                                           tridi_stream_t stream);
 
+/* Self-check of the bounded device waits (no counterpart in the reference):
+   one CTA of num_threads threads (1..1024) waits on an mbarrier for at most
+   limit_cycles SM cycles (1 .. ~2e9, the kernels' own limit).  With
+   arrive != 0 the barrier completes and every wait succeeds; with arrive = 0
+   nothing arrives, every wait runs out, sets TRIDI_DEVERR_WAIT_TIMEOUT in the
+   device status word (tridi_device_status) and returns.  timed_out (device,
+   num_threads ints) receives 1 for each thread whose wait ran out, else 0.
+   Asynchronous on `stream`; faults and hangs nothing. */
+tridi_status tridi_selfcheck_wait(long long limit_cycles, int arrive, int *timed_out, int num_threads,
+                                  tridi_stream_t stream);
+
 /* Allocation-free solve (no counterpart in the reference): for callers that
    cannot call cudaMalloc at solve time, e.g. an application whose device
    memory is all owned by its own pool, or a latency-critical loop that must

@@ -68,6 +68,7 @@ _SIGS["tridi_noalloc_max_unknowns"] = (ctypes.c_long, [])
 _SIGS["tridi_noalloc_last_cuda_error"] = (c_int, [])
 _SIGS["tridi_solve_interleaved_noalloc_f32"] = (c_int, [_P, _P, _P, _P, _P, ctypes.c_long, ctypes.c_long, _P])
 _LL = ctypes.c_longlong
+_SIGS["tridi_selfcheck_wait"] = (c_int, [ctypes.c_longlong, c_int, _P, c_int, _P])
 _SIGS["tridi_selfcheck_df_to_double"] = (c_int, [_P, _P, _P, ctypes.c_long, _P])
 _SIGS["tridi_autotune"] = (c_int, [c_int, ctypes.c_long, ctypes.c_long, _P, POINTER(c_int),
                                    POINTER(ctypes.c_float)])

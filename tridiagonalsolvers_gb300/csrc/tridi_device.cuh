@@ -222,16 +222,24 @@ __device__ __forceinline__ void record_error(unsigned* status, unsigned bit) {
   if (status) atomicOr(status, bit);
 }
 
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* status) {
+// Waits for the phase of `bar` with parity `parity` for at most
+// `limit_cycles` SM cycles; on running out records TRIDI_DEVERR_WAIT_TIMEOUT
+// and returns false.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity, unsigned* status,
+                                              long long limit_cycles) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitLimitCycles) {
+    if (clock64() - t0 > limit_cycles) {
       record_error(status, TRIDI_DEVERR_WAIT_TIMEOUT);
       return false;
     }
   }
   return true;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* status) {
+  return mbar_wait_for(bar, parity, status, kWaitLimitCycles);
 }
 
 // Bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned) from
