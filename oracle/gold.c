@@ -170,3 +170,51 @@ void gold_rel_residual(const float *a, const float *b, const float *c, const flo
     out[s] = dd > 0 ? sqrt(rr) / sqrt(dd) : sqrt(rr);
   }
 }
+
+/* Ragged batches (test infrastructure for the ragged solver, which has no
+   reference counterpart): system s owns rows [off[s], off[s+1]) of the
+   concatenated arrays.  Per system, the FP64 gold Thomas solution (into x64,
+   may be NULL), the relative residual of a given solution (x FP64 or x32
+   FP32, one of them non-NULL) and the forward error max|x - x64| /
+   max|x64| (fwd, may be NULL).  Same Thomas recurrence and residual as the
+   uniform routines above (tridiagonal_gold.h:26-44). */
+void gold_check_ragged(const float *a, const float *b, const float *c, const float *d,
+                       const double *x, const float *x32, const long *off, int m,
+                       double *x64, double *res, double *fwd, int nthreads) {
+  if (nthreads <= 0) nthreads = gold_max_threads();
+  long nmax = 0;
+  for (int s = 0; s < m; s++)
+    if (off[s + 1] - off[s] > nmax) nmax = off[s + 1] - off[s];
+#pragma omp parallel num_threads(nthreads)
+  {
+    double *buf = (double *)malloc(sizeof(double) * 5 * (size_t)(nmax > 0 ? nmax : 1));
+    double *aa = buf, *bb = buf + nmax, *cc = buf + 2 * nmax, *dd = buf + 3 * nmax, *xx = buf + 4 * nmax;
+#pragma omp for schedule(dynamic, 64)
+    for (long s = 0; s < m; s++) {
+      const long lo = off[s], n = off[s + 1] - off[s];
+      double rr = 0, dn = 0, err = 0, big = 0;
+      for (long i = 0; i < n; i++) {
+        const long k = lo + i;
+        const double xi = x ? x[k] : (double)x32[k];
+        double r = (double)d[k] - (double)b[k] * xi;
+        if (i > 0) r -= (double)a[k] * (x ? x[k - 1] : (double)x32[k - 1]);
+        if (i < n - 1) r -= (double)c[k] * (x ? x[k + 1] : (double)x32[k + 1]);
+        rr += r * r;
+        dn += (double)d[k] * (double)d[k];
+        aa[i] = a[k]; bb[i] = b[k]; cc[i] = c[k]; dd[i] = d[k];
+      }
+      if (res) res[s] = dn > 0 ? sqrt(rr) / sqrt(dn) : sqrt(rr);
+      if (n > 0 && (x64 || fwd)) {
+        gold_serial_f64(aa, bb, cc, dd, xx, (int)n);
+        for (long i = 0; i < n; i++) {
+          const double xi = x ? x[lo + i] : (double)x32[lo + i];
+          if (x64) x64[lo + i] = xx[i];
+          if (fabs(xi - xx[i]) > err || xi != xi) err = xi != xi ? INFINITY : fabs(xi - xx[i]);
+          if (fabs(xx[i]) > big) big = fabs(xx[i]);
+        }
+      }
+      if (fwd) fwd[s] = big > 0 ? err / big : err;
+    }
+    free(buf);
+  }
+}

@@ -58,6 +58,8 @@ def gold_lib() -> ctypes.CDLL:
         lib.gold_max_threads.restype = c_int
         lib.gold_solve_f64_from_f32.argtypes = [F32P, F32P, F32P, F32P, F64P, c_int, c_int, c_int, c_int]
         lib.gold_rel_residual.argtypes = [F32P, F32P, F32P, F32P, F64P, F32P, c_int, c_int, c_int, F64P, c_int]
+        lib.gold_check_ragged.argtypes = [F32P, F32P, F32P, F32P, F64P, F32P, POINTER(ctypes.c_long), c_int, F64P,
+                                          F64P, F64P, c_int]
         _gold = lib
     return _gold
 
@@ -163,6 +165,25 @@ def rel_residual(a, b, c, d, x, layout: int = 0, threads: int = 0) -> np.ndarray
         x = np.ascontiguousarray(x, dtype=np.float32)
         lib.gold_rel_residual(*map(_ptr, (a, b, c, d)), None, _ptr(x), n, m, layout, _ptr(out), threads)
     return out
+
+
+def check_ragged(a, b, c, d, x, offsets, threads: int = 0):
+    """Ragged batch (system s = rows offsets[s]..offsets[s+1] of the 1-D
+    arrays): per system the FP64 relative residual of x (FP32 or FP64) and
+    its forward error against the FP64 gold solution.  Returns (res, fwd)."""
+    a, b, c, d = (np.ascontiguousarray(v, dtype=np.float32) for v in (a, b, c, d))
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    m = len(off) - 1
+    total = int(off[-1])
+    res = np.zeros(m, np.float64)
+    fwd = np.zeros(m, np.float64)
+    x = np.ascontiguousarray(x)
+    assert x.size >= total and a.size >= total
+    x64p = _ptr(x) if x.dtype == np.float64 else None
+    x32p = _ptr(np.ascontiguousarray(x, dtype=np.float32)) if x.dtype != np.float64 else None
+    gold_lib().gold_check_ragged(*map(_ptr, (a, b, c, d)), x64p, x32p,
+                                 off.ctypes.data_as(POINTER(ctypes.c_long)), m, None, _ptr(res), _ptr(fwd), threads)
+    return res, fwd
 
 
 def compare_many(x1, x2, eps):

@@ -102,3 +102,21 @@ def test_compare_many_counts_failures_and_nan():
     nf, rms = gold.compare_many(x1, x2, 1e-3)
     assert nf == 2
     assert rms[0] == 0 and abs(rms[1] - 0.5) < 1e-7
+
+
+def test_ragged_check_matches_uniform_routines():
+    """gold_check_ragged on a batch of equal sizes gives the uniform routines'
+    residuals, and zero forward error for the oracle's own FP64 solution."""
+    from tridiagonalsolvers_gb300 import workloads
+
+    m, n = 37, 129
+    a, b, c, d = workloads.dominant(m, n, seed=5)
+    off = np.arange(m + 1, dtype=np.int64) * n
+    x64 = gold.solve_f64(a, b, c, d)
+    res, fwd = gold.check_ragged(a.ravel(), b.ravel(), c.ravel(), d.ravel(), x64.ravel(), off)
+    assert np.array_equal(res, gold.rel_residual(a, b, c, d, x64))
+    assert np.all(fwd == 0)
+    x32 = x64.astype(np.float32)
+    res, fwd = gold.check_ragged(a.ravel(), b.ravel(), c.ravel(), d.ravel(), x32.ravel(), off)
+    assert np.array_equal(res, gold.rel_residual(a, b, c, d, x32))
+    assert np.allclose(fwd, np.abs(x32 - x64).max(axis=1) / np.abs(x64).max(axis=1), rtol=0, atol=0)
