@@ -22,6 +22,17 @@ Lines printed (rank 0, one JSON line):
 --impl reference times the reference's own CPU gold solver (the oracle's
 restatement of tridiagonal_gold.h, bit-identical to it) on every host core,
 on a bounded sample of the same workload.
+
+--gpus N > 1 without a launcher's WORLD_SIZE re-runs this script under
+torch.distributed.run with N ranks, one GPU each: N independent replicas
+(weak scaling, no data-path collective), timed with a barrier on both sides
+and the maximum over ranks.
+
+Code under oracle/ runs in two reported-baseline legs only, never in the
+timed region: cpu_baseline (and the --impl reference arm) time the gold
+Thomas solver; reference_kernels times the reference's own CUDA kernels
+rebuilt for sm_103a (oracle/_ref cubins through oracle/ref_kernels_runner.cpp)
+on the same batch, beside each row of the per-kernel table.
 """
 from __future__ import annotations
 
@@ -89,7 +100,7 @@ class ClockSampler:
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, index: int):
         self.index = index
@@ -122,30 +133,57 @@ class ClockSampler:
         rows = []
         for line in open(self.path):
             f = [v.strip() for v in line.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                rows.append((float(f[1]), float(f[2]), f[5:9]))
+                util = float(f[9])
+            except ValueError:
+                util = 100.0
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9], util))
             except ValueError:
                 continue
         os.unlink(self.path)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
-        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": reasons, "samples": len(rows)}
+        reasons = sorted({names[i] for _, _, r, _ in rows for i, v in enumerate(r) if v.lower() == "active"})
+        # "under load": samples with the GPU busy (all samples if none is)
+        busy = [r for r in rows if r[3] >= 50.0] or rows
+        return {"sm_mhz": statistics.median(r[0] for r in busy), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows), "samples_under_load": len(busy),
+                "sm_mhz_all_samples": statistics.median(r[0] for r in rows)}
+
+
+def rank_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
 
 
 def dist_init(gpus: int):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank, local, world = rank_env()
+    if world != gpus:
+        raise SystemExit(f"bench: --gpus {gpus} but WORLD_SIZE={world}")
     if world > 1:
         import torch.distributed as dist
 
         dist.init_process_group("nccl" if os.environ.get("TRIDI_BENCH_GLOO") != "1" else "gloo")
     return rank, local, world
+
+
+def free_port() -> int:
+    import socket
+
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+def replica_launch_argv(argv: list[str], gpus: int) -> list[str]:
+    """The command that runs this script as `gpus` replica ranks (one process
+    per GPU) under torch.distributed.run on this node."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={gpus}",
+            "--master-addr=127.0.0.1", f"--master-port={free_port()}", str(Path(__file__).resolve()), *argv]
 
 
 def barrier(world):
@@ -161,48 +199,47 @@ def max_over_ranks(v: float, world: int, device) -> float:
 
 
 # ---------------------------------------------------------------------------
-def cpu_gold_rate(a, b, c, d, threads: int, min_seconds: float = 10.0):
-    """Times the oracle's gold Thomas (tridiagonal_gold.h:26-53, restated in
-    oracle/gold.c) on `threads` host threads over repetitions of the batch."""
+# The CPU baselines (cpu_baseline of the GPU arm and the --impl reference arm)
+# time the same sample: the first CPU_SAMPLE_M systems of the batch, one
+# gold Thomas pass over them per step, on every host core.
+CPU_SAMPLE_M = 16384
+
+
+def cpu_gold_steps(a, b, c, d, threads: int, warmup: int, steps: int):
+    """Times `steps` passes of the oracle's gold Thomas (tridiagonal_gold.h:26-53,
+    restated in oracle/gold.c) over the sample on `threads` host threads, after
+    `warmup` untimed passes; returns (unknowns/s, seconds)."""
     from oracle import gold
 
     gold.gold_lib()
-    x = gold.serial_many(a[:64], b[:64], c[:64], d[:64], threads=threads)  # warm up
-    reps, t0 = 0, time.perf_counter()
-    while True:
-        x = gold.serial_many(a, b, c, d, threads=threads)
-        reps += 1
-        el = time.perf_counter() - t0
-        if el >= min_seconds or reps >= 200:
-            break
-    unknowns = reps * a.size
-    return unknowns / el, reps, el
+    for _ in range(max(warmup, 1)):
+        gold.serial_many(a, b, c, d, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        gold.serial_many(a, b, c, d, threads=threads)
+    el = time.perf_counter() - t0
+    return steps * a.size / el, el
 
 
 def run_reference(args):
-    rank, local, world = dist_init(args.gpus)
+    rank, local, world = rank_env()
     if rank != 0:
-        return 0
+        return 0  # replicas: rank 0 alone times the host cores
     from oracle import gold
     from tridiagonalsolvers_gb300 import workloads
 
     cores = gold.gold_lib().gold_max_threads()
-    sample_m = 16384  # a quarter of the batch per step keeps each step ~0.1-1 s
-    a, b, c, d = workloads.dominant(sample_m, N, seed=workloads.SEEDS["c2"])
-    for _ in range(max(args.warmup, 0)):
-        gold.serial_many(a, b, c, d, threads=cores)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        gold.serial_many(a, b, c, d, threads=cores)
-    el = time.perf_counter() - t0
-    rate = args.steps * a.size / el
+    a, b, c, d = workloads.dominant(CPU_SAMPLE_M, N, seed=workloads.SEEDS["c2"])
+    rate, el = cpu_gold_steps(a, b, c, d, cores, args.warmup, args.steps)
+    sample_m = CPU_SAMPLE_M
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "unknowns/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "sample_systems_per_step": sample_m, "system_size": N},
         "cpu_baseline": {"value": rate, "unit": "unknowns/s", "cores": cores, "kind": "port",
-                         "sample": f"{sample_m} of the {M} systems per step (gold Thomas, FP32, OpenMP over systems)"},
+                         "sample": f"{sample_m} of the {M} systems per step (gold Thomas, FP32, OpenMP over systems), "
+                                   f"{args.steps} steps in {el:.2f} s"},
         "e2e": {"value": rate, "unit": "unknowns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -223,6 +260,106 @@ def time_kernel(fn, stream, warmup, iters):
     e1.record(stream)
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / iters
+
+
+def _per_launch_ms(launch, restore, stream, warmup: int, reps: int) -> float:
+    """Median of `reps` single launches timed with CUDA events on `stream`;
+    before each, `restore()` copies the inputs afresh (outside the events), so
+    every launch sees the same data and the same L2 state."""
+    import torch
+
+    times = []
+    for r in range(warmup + reps):
+        restore()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        launch()
+        e1.record(stream)
+        e1.synchronize()
+        if r >= warmup:
+            times.append(e0.elapsed_time(e1))
+    return statistics.median(times)
+
+
+def kernel_table(lib, m: int, n: int, seed: int, dev, peak: float, with_reference: bool, reps: int = 20):
+    """This build's FP32 kernels on one seeded batch of m systems x n unknowns
+    and, beside each, the reference's own kernel for the same launcher
+    rebuilt for sm_103a (its overwrites of a..d undone by a fresh copy before
+    every launch; the same copy precedes ours)."""
+    import torch
+
+    from tridiagonalsolvers_gb300 import workloads
+
+    a, b, c, d = workloads.dominant(m, n, seed=seed)
+    src = [torch.from_numpy(v).to(dev) for v in (a, b, c, d)]
+    work = [torch.empty_like(t) for t in src]
+    ping = [torch.empty_like(t) for t in src]
+    x = torch.empty_like(src[0])
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    wp = [t.data_ptr() for t in (*work, x)]
+
+    def restore():
+        for w, t in zip(work, src):
+            w.copy_(t)
+
+    ours = {"cr": lambda: lib.tridi_cr_f32(*wp, n, m, sp), "pcr": lambda: lib.tridi_pcr_f32(*wp, n, m, sp),
+            "crNBC": lambda: lib.tridi_cr_nbc_f32(*wp, n, m, sp),
+            "crNBC32": lambda: lib.tridi_cr_nbc_f32(*wp, n, m, sp)}
+    rows = [("cr", "cr", 0), ("pcr", "pcr", 0), ("crNBC", "crNBC", 0), ("crNBC32", "crNBC32", 0)]
+    rest = 2
+    while rest <= n // 2:
+        ours[f"crpcr_rest{rest}"] = (lambda r: lambda: lib.tridi_crpcr_f32(*wp, n, m, r, sp))(rest)
+        rows.append((f"crpcr_rest{rest}", "crpcr", rest))
+        rest *= 2
+    r32 = min(32, n // 2)
+    ours[f"crpcrNBC_rest{r32}"] = lambda: lib.tridi_crpcr_nbc_f32(*wp, n, m, r32, sp)
+    rows.append((f"crpcrNBC_rest{r32}", "crpcrNBC", r32))
+    for g in sorted({8, min(n // 2, 512)}):
+        ours[f"pcrGauss_g{g}"] = (lambda gg: lambda: lib.tridi_pcr_thomas_f32(*wp, n, m, gg, sp))(g)
+        rows.append((f"pcrGauss_g{g}", "pcrGauss", g))
+    rk = None
+    if with_reference:
+        try:
+            from oracle.gold import RefKernels
+
+            rk = RefKernels() if RefKernels.available() else None
+        except Exception:  # the reference kernels were not built on this machine
+            rk = None
+    out = {"reference_kernels": "oracle/_ref cubins (reference sources rebuilt for sm_103a)" if rk else
+           "not available (reference kernels not built)"}
+
+    def fig(ms):
+        gbs = BYTES_PER_UNKNOWN * m * n / (ms * 1e-3) / 1e9
+        return {"ms": round(ms, 5), "unknowns_per_s": m * n / (ms * 1e-3), "gbs": round(gbs, 1),
+                "frac": round(gbs / peak, 4)}
+
+    for name, kind, param in rows:
+        row = {}
+        t = _per_launch_ms(lambda: _check_status(ours[name](), name), restore, stream, 3, reps)
+        row["ours"] = fig(t)
+        if rk is not None:
+            try:
+                if kind == "pcrGauss":
+                    if n > 1024:
+                        raise ValueError("the reference's small pcrGauss path takes n <= 1024")
+                    launch = lambda: rk.pcr_gauss(*work, *ping, n, m, param, stream.cuda_stream)
+                else:
+                    launch = lambda: rk.solve(kind, *work, x, n, m, param, stream.cuda_stream)
+                tr = _per_launch_ms(launch, restore, stream, 3, reps)
+                row["reference"] = fig(tr)
+                row["speedup"] = round(tr / t, 3)
+            except Exception as e:  # a shape the reference kernel does not launch
+                row["reference"] = {"error": str(e)[:100]}
+        out[name] = row
+    return out
+
+
+def _check_status(st, what):
+    from tridiagonalsolvers_gb300 import _lib
+
+    _lib.check(st, what)
 
 
 def run_gpu(args):
@@ -298,9 +435,10 @@ def run_gpu(args):
         if not res < 2e-6:
             raise SystemExit(f"bench: drop-in cr result fails the residual check (residual {res:.2e})")
 
-    # ---- per-kernel table on the same batch (outside the timed region) ----
+    # ---- per-kernel tables (outside the timed region) ----
     peak, peak_kind = measured_peaks()
     kernels = {}
+    tables = {}
     if rank == 0 and not args.no_table:
         cands = [("cr", lambda: lib.tridi_cr_f32(*ptrs, N, M, sp)),
                  ("crNBC", lambda: lib.tridi_cr_nbc_f32(*ptrs, N, M, sp)),
@@ -316,16 +454,27 @@ def run_gpu(args):
             gbs = BYTES_PER_UNKNOWN * unknowns / (t * 1e-3) / 1e9
             kernels[name] = {"ms": round(t, 5), "unknowns_per_s": unknowns / (t * 1e-3), "gbs": round(gbs, 1),
                              "frac": round(gbs / peak, 4)}
+        # every plain FP32 shape of the benchmark definitions, each row beside
+        # the reference's own kernel rebuilt for sm_103a (a reported baseline)
+        with ClockSampler(local) as tclk:
+            for (m_, n_, seed_) in ((512, 512, "c1"), (M, N, "c2"), (16384, 1024, "c2b")):
+                tables[f"{m_}x{n_}"] = kernel_table(lib, m_, n_, workloads.SEEDS[seed_], dev, peak,
+                                                    with_reference=not args.no_reference_kernels)
+        tables["clocks"] = tclk.summary()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import gold
 
         cores = gold.gold_lib().gold_max_threads()
-        sm = 8192
-        rate, reps, el = cpu_gold_rate(a[:sm], b[:sm], c[:sm], d[:sm], cores, min_seconds=3.0)
+        sm = CPU_SAMPLE_M
+        sample = [np.ascontiguousarray(v[:sm]) for v in (a, b, c, d)]
+        _, one = cpu_gold_steps(*sample, cores, 3, 1)
+        reps = max(20, int(np.ceil(10.0 / max(one, 1e-3))))
+        rate, el = cpu_gold_steps(*sample, cores, 0, reps)
         cpu = {"value": rate, "unit": "unknowns/s", "cores": cores, "kind": "port",
-               "sample": f"{reps} x {sm} of the {M} systems (gold Thomas FP32, {el:.1f} s wall on {cores} threads)"}
+               "sample": f"{reps} passes over {sm} of the {M} systems (gold Thomas FP32, {el:.1f} s wall on "
+                         f"{cores} threads; the --impl reference arm times the same sample)"}
 
     if rank == 0:
         achieved = BYTES_PER_UNKNOWN * unknowns / (ms * 1e-3) / 1e9
@@ -347,6 +496,7 @@ def run_gpu(args):
             "gpu_launches": args.steps,
             "device_status": status,
             "kernels": kernels,
+            "kernel_tables": tables,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -384,6 +534,7 @@ def run_large(args):
     def step():
         _lib.check(lib.tridi_solve_large_f32(*ptrs, n, m, 1, ws.data_ptr(), wsb, sp), "tridi_solve_large_f32")
 
+    clk = ClockSampler(0).__enter__()
     ms = time_kernel(step, stream, args.warmup, args.steps)
     x64 = torch.empty(n * m, dtype=torch.float64, device=dev)
     rwsb = lib.tridi_refine_workspace_bytes(n, m, 1)
@@ -401,6 +552,7 @@ def run_large(args):
         lib.tridi_set_tunable(4, 2)
         rms64 = time_kernel(rstep, stream, 1, max(1, args.steps // 5))
         lib.tridi_set_tunable(4, 0)
+    clk.__exit__(None, None, None)
     peak, kind = measured_peaks()
     unknowns = n * m
     line = {
@@ -418,6 +570,7 @@ def run_large(args):
         "refined_fp64": {"value": unknowns / (rms64 * 1e-3), "ms_per_step": rms64, "sweeps": sweeps.value,
                          "rel_residual": rel.value, "tol": 1e-10, "frac_of_plain": ms / rms64,
                          "residual_arithmetic": "native FP64"},
+        "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -456,7 +609,9 @@ def run_ragged(args):
     plan = RaggedPlan(off, device=dev)
     x = torch.zeros(padded(total), dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
+    clk = ClockSampler(0).__enter__()
     ms = time_kernel(lambda: plan.solve(*t, x=x), stream, args.warmup, args.steps)
+    clk.__exit__(None, None, None)
     # the refinement's own choice per size bucket (timed on the fused refinement)
     tuned_refine = {}
     if not args.no_autotune:
@@ -465,6 +620,7 @@ def run_ragged(args):
                 tuned_refine[str(k)] = autotune.tune("ragged_refine", k)[0]
     rplan = RaggedPlan(off, device=dev, refine=True)
     refined = {}
+    rclk = ClockSampler(0).__enter__()
     for mode in ("df", "fp64"):
         ref = RaggedRefiner(rplan, *t, sweeps=args.sweeps, graph=True, residual=mode)
         rms = time_kernel(ref.launch, stream, 3, max(3, args.steps // 2))
@@ -473,6 +629,7 @@ def run_ragged(args):
                          "rel_residual": rel, "tol": 1e-10, "frac_of_plain": ms / rms, "cuda_graph": True,
                          "residual_arithmetic": {"df": "double-float (FP32 pairs)", "fp64": "native FP64"}[mode]}
         del ref
+    rclk.__exit__(None, None, None)
     peak, kind = measured_peaks()
     line = {
         "metric": METRIC, "value": total / (ms * 1e-3), "unit": "unknowns/s", "n_gpus": 1, "steps": args.steps,
@@ -491,6 +648,8 @@ def run_ragged(args):
                      "traffic_note": "ncu dram bytes per row of a 20000-system capture, scaled to this batch"},
         "refined": refined["df"],
         "refined_fp64": refined["fp64"],
+        "clocks": clk.summary(),
+        "clocks_refined": rclk.summary(),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -548,6 +707,7 @@ def run_serve(args):
     # of the request and result arrays touched), as a serving loop that has
     # been running would be
     serve_once([0.0] * len(pool))
+    clk = ClockSampler(0).__enter__()
     wall, infos = serve_once([0.0] * len(pool))
     sat = total / wall
     def lat(infos):
@@ -618,6 +778,7 @@ def run_serve(args):
     for _ in range(5):
         e2e_pageable()
     e2e_pg_s = (time.perf_counter() - t0) / 5
+    clk.__exit__(None, None, None)
     plain_dev = total / (ms_dev * 1e-3)
     plain_e2e = total / e2e_s
     plain_e2e_pg = total / e2e_pg_s
@@ -641,6 +802,7 @@ def run_serve(args):
                                  "served_frac_of_plain_e2e_pinned": sat / plain_e2e,
                                  "served_frac_of_plain_e2e_pageable": sat / plain_e2e_pg,
                                  "served_frac_of_plain_device": sat / plain_dev},
+        "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -660,6 +822,8 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-table", action="store_true", help="skip the per-kernel table")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-reference-kernels", action="store_true",
+                    help="per-kernel tables without the reference's own kernels beside them")
     ap.add_argument("--workload", default="batch", choices=["batch", "large", "ragged", "serve"],
                     help="batch: 65536 x 256 (default, the headline); large: 1024 x 65536 interleaved; "
                          "ragged: 100000 ADI systems of 32..8192 unknowns; serve: a served request stream")
@@ -674,6 +838,10 @@ def main():
     ap.add_argument("--large-n", type=int, default=65536, help="system size of the large workload")
     ap.add_argument("--no-refine", action="store_true", help="large workload: plain solve only")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # N independent replicas, one process per GPU
+        argv = replica_launch_argv(sys.argv[1:], args.gpus)
+        return subprocess.run(argv).returncode
     if args.warmup < 3 and args.impl == "native":
         args.warmup = 3
     if args.impl == "reference":
