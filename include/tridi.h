@@ -63,7 +63,9 @@ tridi_status tridi_init(void);
 tridi_status tridi_device_status(unsigned *bits, int reset);
 
 /* Launch-shape tunables (process-wide; 0 = automatic).  Used by the
-   autotuner and by experiments; they never change results, only speed. */
+   autotuner and by experiments; they change speed, and at most the rounding
+   of results (TRIDI_TUNE_PCR_KERNEL, TRIDI_TUNE_RESIDUAL), never the
+   algorithm. */
 #define TRIDI_TUNE_STAGES 1     /* cp.async.bulk pipeline stages per CTA (1..8) */
 #define TRIDI_TUNE_CRPCR_REST 2 /* switch level of the CR-PCR correction solves */
 #define TRIDI_TUNE_CR_ROWS 3    /* rows per thread of the CR/PCR/CR-PCR kernels (2, 4, 8, 16) */
@@ -82,6 +84,9 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
                                      shared-memory kernel always */
 #define TRIDI_TUNE_DROPIN_CHUNK 9 /* host-pointer launchers: KiB of each coefficient array per pipelined chunk
                                      (0 = 8192) */
+#define TRIDI_TUNE_PCR_KERNEL 10  /* FP32 PCR on 64..512 unknowns: 0/1 = the two-phase kernel (rows transposed
+                                     once between the register phases), 2 = the hybrid warp kernel (the
+                                     same algorithm; results differ in rounding only) */
 tridi_status tridi_set_tunable(int key, int value);
 int tridi_get_tunable(int key);
 

@@ -2,6 +2,7 @@
 // (hybrid.cuh).  Replaces the device work of cr() (cr_app.cu:4), pcr()
 // (pcr_app.cu:5) and crpcr() (crpcr_app.cu:5).
 #include "hybrid.cuh"
+#include "pcr_twophase.cuh"
 #include "runtime.h"
 
 namespace tridi {
@@ -124,6 +125,42 @@ cudaError_t launch_one(const HybridParams& p0, const DeviceInfo& dev, cudaStream
   return cudaGetLastError();
 }
 
+// FP32 PCR on 64..512 unknowns: the two-phase kernel (pcr_twophase.cuh).
+// Each array is a tensor of rows of 32 values; a warp tile is a box of 16
+// such rows.
+template <int N>
+cudaError_t launch_pcr_twophase(const HybridParams& p, const DeviceInfo& dev, cudaStream_t stream) {
+  auto kern = pcr_twophase_kernel<N>;
+  constexpr int kThreads = kPcr2Warps * 32;
+  const uint64_t rows = (uint64_t)p.m * N / 32;
+  CUtensorMap ma, mb, mc, md;
+  if (!make_tensor_map_2d(&ma, static_cast<const float*>(p.a), 32, rows, 128, 32, kPcr2TileFloats / 32, true) ||
+      !make_tensor_map_2d(&mb, static_cast<const float*>(p.b), 32, rows, 128, 32, kPcr2TileFloats / 32, true) ||
+      !make_tensor_map_2d(&mc, static_cast<const float*>(p.c), 32, rows, 128, 32, kPcr2TileFloats / 32, true) ||
+      !make_tensor_map_2d(&md, static_cast<const float*>(p.d), 32, rows, 128, 32, kPcr2TileFloats / 32, true))
+    return cudaErrorInvalidValue;
+  if (kPcr2Smem > (size_t)dev.max_smem_optin) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPcr2Smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, kPcr2Smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  const long tiles = ((long)p.m * N + kPcr2TileFloats - 1) / kPcr2TileFloats;
+  long grid = (long)per_sm * dev.sm_count;
+  if (grid * kPcr2Warps > tiles) grid = (tiles + kPcr2Warps - 1) / kPcr2Warps;
+  kern<<<(unsigned)grid, kThreads, kPcr2Smem, stream>>>(p, ma, mb, mc, md);
+  return cudaGetLastError();
+}
+
+template <class T>
+bool pcr_twophase_applies(const HybridParams& p) {
+  if constexpr (sizeof(T) != 4) return false;
+  return p.stride == 1 && (p.n == 64 || p.n == 128 || p.n == 256 || p.n == 512) && aligned16(p.a) &&
+         aligned16(p.b) && aligned16(p.c) && aligned16(p.d) && (long)p.m * p.n / 32 < (1L << 31) &&
+         tunable(TRIDI_TUNE_PCR_KERNEL) != 2;
+}
+
 template <class T>
 tridi_status solve_hybrid(const T* a, const T* b, const T* c, const T* d, T* x, int n, int m, int stride,
                           tridi_stream_t stream) {
@@ -142,6 +179,16 @@ tridi_status solve_hybrid(const T* a, const T* b, const T* c, const T* d, T* x, 
   p.status = dev->status;
   cudaStream_t s = as_stream(stream);
   cudaError_t e = cudaErrorInvalidValue;
+  if constexpr (sizeof(T) == 4) {
+    if (pcr_twophase_applies<T>(p)) {
+      switch (n) {
+        case 64: return cuda_status(launch_pcr_twophase<64>(p, *dev, s));
+        case 128: return cuda_status(launch_pcr_twophase<128>(p, *dev, s));
+        case 256: return cuda_status(launch_pcr_twophase<256>(p, *dev, s));
+        default: return cuda_status(launch_pcr_twophase<512>(p, *dev, s));
+      }
+    }
+  }
   const int ls = stride < sh.K ? stride : 0;
 #define TRIDI_LAUNCH_LS(KK, WW, LS) \
   if (sh.K == KK && sh.warp == WW && ls == LS) e = launch_one<T, KK, WW, LS>(p, *dev, s);

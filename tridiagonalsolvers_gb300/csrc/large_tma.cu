@@ -64,14 +64,6 @@ __device__ __forceinline__ void put_separator(float* red, long S, long o, const 
   red[3 * S + o] = sep.d - sep.a * lD - sep.c * nD;
 }
 
-__device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
-          "r"(smem_addr(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
-      : "memory");
-}
-
 // Forward elimination of one lane's column (rows 0..k-2 at stride 32 words)
 // into registers: the normalised c', a', d' of every interior row.  The
 // stage can go back to the producer as soon as this (and the read of the
@@ -262,33 +254,9 @@ __global__ void __launch_bounds__(256) large_tile_boundary_kernel(LtParams p) {
                 b[(kBndLast + 2) * p.BS], nD, nC, nA);
 }
 
-// The driver's tensor-map encoder, looked up through the runtime once (the
-// library does not link the driver library itself, so it loads on machines
-// without one).
-PFN_cuTensorMapEncodeTiled_v12000 encoder() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  });
-  return fn;
-}
-
 bool make_map(CUtensorMap* map, const float* base, long n, long m) {
-  const auto enc = encoder();
-  if (!enc) return false;
-  const cuuint64_t dims[2] = {(cuuint64_t)m, (cuuint64_t)n};
-  const cuuint64_t strides[1] = {(cuuint64_t)m * sizeof(float)};
-  const cuuint32_t box[2] = {(cuuint32_t)kTileCols, (cuuint32_t)kTileRows};
-  const cuuint32_t elem[2] = {1, 1};
-  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, elem,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  return make_tensor_map_2d(map, base, (uint64_t)m, (uint64_t)n, (uint64_t)m * sizeof(float), kTileCols, kTileRows,
+                            false);
 }
 
 }  // namespace

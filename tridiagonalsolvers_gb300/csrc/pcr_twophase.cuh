@@ -1,0 +1,301 @@
+// Parallel cyclic reduction for FP32 systems of 64..512 unknowns in two
+// register phases around one transpose (replaces the device work of pcr(),
+// pcr_app.cu:5 / pcrKernel, pcr_kernel.cu:1-77, at these sizes).
+//
+// The algorithm is the reference's: log2(n/2) PCR steps with distances
+// 1, 2, ..., n/4, each eliminating every row's couplings against its
+// neighbours at that distance, then n/2 independent 2x2 systems (i, i+n/2).
+// Rows are kept normalised (divided by their diagonal, b = 1): each step
+// forms me - a*L - c*R from the normalised neighbours L, R and normalises the
+// result with one reciprocal, so three words per row move between lanes and
+// each row costs one reciprocal per step.
+//
+// Mapping (n = 16 * LPS, LPS lanes per system, 32 / LPS systems per warp):
+//   phase A  lane p holds rows 16p .. 16p+15.  Steps of distance 1, 2, 4, 8
+//            run inside the lane; a row whose neighbour lies in the next or
+//            previous lane gets it over one shuffle (3 words).
+//   transpose  the normalised rows go through the warp's staging buffer
+//            (16-byte stores, XOR-swizzled so that neither the stores nor the
+//            4-byte loads of the other side conflict on banks), and lane c
+//            takes rows c + LPS*s, s = 0 .. 15.
+//   phase B  distances 16 .. n/4 move only the slot index s (by 16/LPS ..)
+//            and stay inside the lane (n = 512: distance 16 is a lane
+//            exchange with lane c ^ 16); neighbours beyond the system's ends
+//            have coupling exactly zero and are skipped at compile time.  The
+//            closing 2x2 systems pair slots s and s+8 of the same lane.
+// x is written straight from phase B: for a fixed s the LPS lanes of a system
+// store LPS consecutive unknowns.
+// Input rows arrive through a private two-buffer ring per warp: a tile (32/LPS
+// systems, 512 consecutive values of each array) is one 16 x 128-byte box of
+// each array's tensor map, copied by cp.async.bulk.tensor with the 128-byte
+// swizzle, so the 16-byte loads of a lane's 64 bytes are conflict-free with
+// no register shuffling (lane l reads box row l/2, chunks 4(l%2)+q, stored at
+// chunk (4(l%2)+q) ^ (l/2 mod 8)).  The buffer just read into registers is
+// the transpose scratch until it is refilled.
+#pragma once
+#include "tridi_device.cuh"
+
+namespace tridi {
+
+namespace pcr2 {
+
+constexpr int kRows = 16;  // rows a lane holds in either phase
+
+// One normalised row: a x[i-dl] + x[i] + c x[i+dl] = d.
+struct NR {
+  float a, c, d;
+};
+
+__device__ __forceinline__ float rcp_approx(float v) { return __fdividef(1.0f, v); }
+
+// me - me.a * L - me.c * R, normalised.
+__device__ __forceinline__ NR step_both(const NR& me, const NR& L, const NR& R) {
+  const float b = fmaf(-me.c, R.a, fmaf(-me.a, L.c, 1.0f));
+  const float d = fmaf(-me.c, R.d, fmaf(-me.a, L.d, me.d));
+  const float ib = rcp_approx(b);
+  return {(-me.a * L.a) * ib, (-me.c * R.c) * ib, d * ib};
+}
+// The left neighbour lies beyond the system's first row: its coupling me.a is
+// exactly zero.
+__device__ __forceinline__ NR step_right(const NR& me, const NR& R) {
+  const float b = fmaf(-me.c, R.a, 1.0f);
+  const float d = fmaf(-me.c, R.d, me.d);
+  const float ib = rcp_approx(b);
+  return {0.0f, (-me.c * R.c) * ib, d * ib};
+}
+// The right neighbour lies beyond the system's last row.
+__device__ __forceinline__ NR step_left(const NR& me, const NR& L) {
+  const float b = fmaf(-me.a, L.c, 1.0f);
+  const float d = fmaf(-me.a, L.d, me.d);
+  const float ib = rcp_approx(b);
+  return {(-me.a * L.a) * ib, 0.0f, d * ib};
+}
+
+__device__ __forceinline__ NR shfl_up_nr(const NR& v, int width) {
+  return {__shfl_up_sync(kFull, v.a, 1, width), __shfl_up_sync(kFull, v.c, 1, width),
+          __shfl_up_sync(kFull, v.d, 1, width)};
+}
+__device__ __forceinline__ NR shfl_down_nr(const NR& v, int width) {
+  return {__shfl_down_sync(kFull, v.a, 1, width), __shfl_down_sync(kFull, v.c, 1, width),
+          __shfl_down_sync(kFull, v.d, 1, width)};
+}
+__device__ __forceinline__ NR shfl_xor_nr(const NR& v, int mask) {
+  return {__shfl_xor_sync(kFull, v.a, mask), __shfl_xor_sync(kFull, v.c, mask), __shfl_xor_sync(kFull, v.d, mask)};
+}
+
+// Phase A step of distance DL (1..8) on the lane's contiguous rows.  Rows are
+// visited by residue j mod DL, so each old row dies right after its last use.
+// Lanes at the system's ends receive their own row from the shuffle: its
+// coupling there is exactly zero (a[0] = c[n-1] = 0 and, by induction over
+// the steps, every row closer to an end than the step distance).
+template <int DL, int LPS>
+__device__ __forceinline__ void phase_a_step(NR (&w)[kRows]) {
+  NR o[kRows];
+#pragma unroll
+  for (int j = 0; j < DL; ++j) {
+    const NR fromL = shfl_up_nr(w[kRows - DL + j], LPS);   // previous lane's row 16-DL+j
+    const NR fromR = shfl_down_nr(w[j], LPS);              // next lane's row j
+#pragma unroll
+    for (int q = j; q < kRows; q += DL) {
+      const NR& L = q >= DL ? w[q - DL] : fromL;
+      const NR& R = q + DL < kRows ? w[q + DL] : fromR;
+      o[q] = step_both(w[q], L, R);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kRows; ++q) w[q] = o[q];
+}
+
+// Phase B step moving the slot index by K (rows c + LPS*s: distance K*LPS).
+template <int K>
+__device__ __forceinline__ void phase_b_step(NR (&w)[kRows]) {
+  NR o[kRows];
+#pragma unroll
+  for (int s = 0; s < kRows; ++s) {
+    if (s >= K && s + K < kRows) o[s] = step_both(w[s], w[s - K], w[s + K]);
+    else if (s + K < kRows) o[s] = step_right(w[s], w[s + K]);
+    else o[s] = step_left(w[s], w[s - K]);
+  }
+#pragma unroll
+  for (int s = 0; s < kRows; ++s) w[s] = o[s];
+}
+
+// n = 512 only: distance 16 after the transpose (lane c holds rows c + 32 s):
+// the neighbours at +-16 are lane c ^ 16, in slot s (the nearer side) or
+// s -/+ 1 (the farther side).
+__device__ __forceinline__ void phase_b_xor16(NR (&w)[kRows], int lane) {
+  NR px[kRows];
+#pragma unroll
+  for (int s = 0; s < kRows; ++s) px[s] = shfl_xor_nr(w[s], 16);
+  const bool lower = lane < 16;  // row c + 32 s, c < 16: R = partner slot s, L = partner slot s-1
+  NR o[kRows];
+#pragma unroll
+  for (int s = 0; s < kRows; ++s) {
+    const NR Lf = s > 0 ? px[s - 1] : w[s];       // (beyond the first row when s = 0: coupling zero)
+    const NR Rf = s + 1 < kRows ? px[s + 1] : w[s];  // (beyond the last row)
+    const NR L = lower ? Lf : px[s];
+    const NR R = lower ? px[s] : Rf;
+    o[s] = step_both(w[s], L, R);
+  }
+#pragma unroll
+  for (int s = 0; s < kRows; ++s) w[s] = o[s];
+}
+
+// Scratch index of row r of one system's word array: the rows of phase-A
+// lane p = r / 16 form a 64-byte block whose four 16-byte chunks are
+// XOR-swizzled by (p / 2) mod 4.
+__device__ __forceinline__ int swz(int r) {
+  const int p = r >> 4, j = r & 15;
+  return (p << 4) + ((((j >> 2) ^ (p >> 1)) & 3) << 2) + (j & 3);
+}
+
+}  // namespace pcr2
+
+// Shared memory of one CTA of kPcr2Warps warps: barriers, then (1024-byte
+// aligned, as the 128-byte swizzle requires) two ring buffers per warp of
+// 4 arrays x 2 KiB.
+constexpr int kPcr2Warps = 4;
+constexpr int kPcr2TileFloats = 512;  // values of one array in a warp tile
+constexpr size_t kPcr2Smem = 128 + 1024 + (size_t)kPcr2Warps * 2 * 4 * kPcr2TileFloats * sizeof(float);
+
+// One launch: every warp streams its own tiles of 32/LPS systems.
+template <int N>
+__global__ void __launch_bounds__(kPcr2Warps * 32, 3)
+    pcr_twophase_kernel(HybridParams p, const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb,
+                        const __grid_constant__ CUtensorMap mc, const __grid_constant__ CUtensorMap md) {
+  using namespace pcr2;
+  constexpr int LPS = N / kRows;  // lanes per system
+  constexpr int SPW = 32 / LPS;   // systems per warp tile
+  constexpr int TF = kPcr2TileFloats;  // = SPW * N
+  constexpr int BUF = 4 * TF;          // floats per ring buffer (a, b, c, d of a tile)
+  constexpr int SYS_STRIDE = 3 * N + LPS;  // transpose scratch per system (padded: no bank conflicts)
+  static_assert(N >= 64 && N <= 512 && SPW * N == TF && SPW * SYS_STRIDE <= BUF, "pcr_twophase: 64 <= n <= 512");
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + 2 * warp;
+  const uint32_t base = smem_addr(smem);
+  const uint32_t ring = (base + 128 + 1023) & ~1023u;
+  float* buf = reinterpret_cast<float*>(smem + (ring - base)) + (size_t)2 * warp * BUF;
+  float* gx = static_cast<float*>(p.x);
+  const long tiles = ((long)p.m + SPW - 1) / SPW;
+  const long first = (long)blockIdx.x * (blockDim.x >> 5) + warp;
+  const long step = (long)gridDim.x * (blockDim.x >> 5);
+  if (lane == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_fence_init();
+  }
+  __syncwarp();
+  const auto issue = [&](long tile, int s) {  // lane 0; the last tile's box reads zeros beyond the batch
+    float* st = buf + s * BUF;
+    const int row = (int)(tile * (TF / 32));
+    mbar_arrive_expect_tx(&bars[s], 4 * TF * sizeof(float));
+    tma_load_2d(st + 0 * TF, &ma, 0, row, &bars[s]);
+    tma_load_2d(st + 1 * TF, &mb, 0, row, &bars[s]);
+    tma_load_2d(st + 2 * TF, &mc, 0, row, &bars[s]);
+    tma_load_2d(st + 3 * TF, &md, 0, row, &bars[s]);
+  };
+  if (lane == 0 && first < tiles) issue(first, 0);
+  const int g = lane / LPS, t = lane % LPS;
+  // this lane's four swizzled 16-byte chunks in a box (row lane/2)
+  int chunk[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) chunk[q] = (lane >> 1) * 32 + ((((lane & 1) * 4 + q) ^ ((lane >> 1) & 7)) << 2);
+  int k = 0;
+  for (long tile = first; tile < tiles; tile += step, ++k) {
+    const int s = k & 1;
+    // the other buffer was last used (transpose scratch) one tile ago and
+    // the warp synchronised since: refill it with the next tile
+    if (lane == 0 && tile + step < tiles) {
+      fence_proxy_async_smem();
+      issue(tile + step, s ^ 1);
+    }
+    if (!mbar_wait(&bars[s], (k >> 1) & 1, p.status)) break;
+    float* st = buf + s * BUF;
+    NR w[kRows];
+    {
+      float v[4][kRows];  // a, b, c, d of the lane's 16 rows
+#pragma unroll
+      for (int arr = 0; arr < 4; ++arr)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float4 f = *reinterpret_cast<const float4*>(st + arr * TF + chunk[q]);
+          v[arr][4 * q] = f.x; v[arr][4 * q + 1] = f.y; v[arr][4 * q + 2] = f.z; v[arr][4 * q + 3] = f.w;
+        }
+      if (t == 0) v[0][0] = 0.0f;               // a[0] is not part of the system
+      if (t == LPS - 1) v[2][kRows - 1] = 0.0f;  // nor is c[n-1]
+#pragma unroll
+      for (int q = 0; q < kRows; ++q) {
+        const float ib = rcp_approx(v[1][q]);
+        w[q] = NR{v[0][q] * ib, v[2][q] * ib, v[3][q] * ib};
+      }
+    }
+    __syncwarp();  // the buffer is read: it is the transpose scratch from here on
+
+    // ---- phase A: distances 1, 2, 4, 8 ----
+    phase_a_step<1, LPS>(w);
+    phase_a_step<2, LPS>(w);
+    phase_a_step<4, LPS>(w);
+    phase_a_step<8, LPS>(w);
+
+    // ---- transpose: lane t of system g now takes rows t + LPS * s ----
+    {
+      float* sa = st + g * SYS_STRIDE;
+      float* sc = sa + N;
+      float* sd = sa + 2 * N;
+      const int rb = t * kRows;  // this lane's first phase-A row
+#pragma unroll
+      for (int q4 = 0; q4 < kRows / 4; ++q4) {
+        const int o = swz(rb + 4 * q4);
+        *reinterpret_cast<float4*>(sa + o) = make_float4(w[4 * q4].a, w[4 * q4 + 1].a, w[4 * q4 + 2].a, w[4 * q4 + 3].a);
+        *reinterpret_cast<float4*>(sc + o) = make_float4(w[4 * q4].c, w[4 * q4 + 1].c, w[4 * q4 + 2].c, w[4 * q4 + 3].c);
+        *reinterpret_cast<float4*>(sd + o) = make_float4(w[4 * q4].d, w[4 * q4 + 1].d, w[4 * q4 + 2].d, w[4 * q4 + 3].d);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < kRows; ++q) {
+        const int o = swz(t + LPS * q);
+        w[q] = NR{sa[o], sc[o], sd[o]};
+      }
+      // every lane's stores and loads of the buffer are ordered before the
+      // bulk copy that refills it (issued by lane 0 after the next wait)
+      fence_proxy_async_smem();
+      __syncwarp();
+    }
+
+    // ---- phase B: distances 16 .. n/4 inside the lane ----
+    if constexpr (N == 512) {
+      phase_b_xor16(w, lane);
+      phase_b_step<1>(w);
+      phase_b_step<2>(w);
+      phase_b_step<4>(w);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 3; ++e) {
+        const int dist = 16 << e;  // rows
+        if (dist <= N / 4) {
+          if (dist / LPS == 1) phase_b_step<1>(w);
+          else if (dist / LPS == 2) phase_b_step<2>(w);
+          else phase_b_step<4>(w);
+        }
+      }
+    }
+
+    // ---- 2x2 systems (s, s + 8): x_u + c_u x_l = d_u, a_l x_u + x_l = d_l ----
+    const long sys = tile * SPW + g;
+    if (sys < p.m) {
+      float* dst = gx + sys * N + t;
+#pragma unroll
+      for (int q = 0; q < kRows / 2; ++q) {
+        const NR& u = w[q];
+        const NR& l = w[q + kRows / 2];
+        const float xu = (u.d - u.c * l.d) * rcp_approx(fmaf(-u.c, l.a, 1.0f));
+        const float xl = fmaf(-l.a, xu, l.d);
+        dst[LPS * q] = xu;
+        dst[LPS * (q + kRows / 2)] = xl;
+      }
+    }
+  }
+}
+
+}  // namespace tridi

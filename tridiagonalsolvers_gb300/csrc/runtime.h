@@ -2,6 +2,7 @@
 // shared-memory limit), the per-device status word that bounded device waits
 // report into, CUDA error capture, and the stream type conversion.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -51,6 +52,16 @@ inline int ilog2(long v) {
 // Pipeline depth for a tiled kernel: the tunable if set, else `fallback`,
 // reduced until the shared memory fits the device.
 int pick_stages(size_t fixed_bytes, size_t stage_bytes, int fallback, const DeviceInfo& dev);
+
+// A 2-D FP32 tensor map for cp.async.bulk.tensor: `outer` rows of `inner`
+// elements, consecutive rows `row_bytes` apart, copied in boxes of
+// box_inner x box_outer elements; swizzle128 selects the 128-byte swizzle
+// (16-byte chunk c of box row r lands at chunk c ^ (r mod 8); the shared
+// destination must then be 1024-byte aligned).  Out-of-range box elements
+// read as zero.  False if the driver's encoder is unavailable or refuses the
+// arguments.
+bool make_tensor_map_2d(CUtensorMap* map, const float* base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+                        uint32_t box_inner, uint32_t box_outer, bool swizzle128);
 
 // Largest system the uniform partition solver (tridi_solve_*) takes: 512
 // threads of 17 rows (FP32) or 9 rows (FP64) each.
