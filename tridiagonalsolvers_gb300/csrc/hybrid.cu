@@ -128,9 +128,9 @@ cudaError_t launch_one(const HybridParams& p0, const DeviceInfo& dev, cudaStream
 // FP32 PCR on 64..512 unknowns: the two-phase kernel (pcr_twophase.cuh).
 // Each array is a tensor of rows of 32 values; a warp tile is a box of 16
 // such rows.
-template <int N>
+template <int N, bool PAIRED>
 cudaError_t launch_pcr_twophase(const HybridParams& p, const DeviceInfo& dev, cudaStream_t stream) {
-  auto kern = pcr_twophase_kernel<N>;
+  auto kern = pcr_twophase_kernel<N, PAIRED>;
   constexpr int kThreads = kPcr2Warps * 32;
   const uint64_t rows = (uint64_t)p.m * N / 32;
   CUtensorMap ma, mb, mc, md;
@@ -181,11 +181,16 @@ tridi_status solve_hybrid(const T* a, const T* b, const T* c, const T* d, T* x, 
   cudaError_t e = cudaErrorInvalidValue;
   if constexpr (sizeof(T) == 4) {
     if (pcr_twophase_applies<T>(p)) {
+      const bool paired = tunable(TRIDI_TUNE_PCR_KERNEL) != 3;
       switch (n) {
-        case 64: return cuda_status(launch_pcr_twophase<64>(p, *dev, s));
-        case 128: return cuda_status(launch_pcr_twophase<128>(p, *dev, s));
-        case 256: return cuda_status(launch_pcr_twophase<256>(p, *dev, s));
-        default: return cuda_status(launch_pcr_twophase<512>(p, *dev, s));
+        case 64: return cuda_status(paired ? launch_pcr_twophase<64, true>(p, *dev, s)
+                                           : launch_pcr_twophase<64, false>(p, *dev, s));
+        case 128: return cuda_status(paired ? launch_pcr_twophase<128, true>(p, *dev, s)
+                                            : launch_pcr_twophase<128, false>(p, *dev, s));
+        case 256: return cuda_status(paired ? launch_pcr_twophase<256, true>(p, *dev, s)
+                                            : launch_pcr_twophase<256, false>(p, *dev, s));
+        default: return cuda_status(paired ? launch_pcr_twophase<512, true>(p, *dev, s)
+                                           : launch_pcr_twophase<512, false>(p, *dev, s));
       }
     }
   }

@@ -46,7 +46,15 @@ struct NR {
   float a, c, d;
 };
 
-__device__ __forceinline__ float rcp_approx(float v) { return __fdividef(1.0f, v); }
+// Reciprocal by the hardware's approximate reciprocal (PTX rcp.approx.ftz.f32:
+// at most 1 ulp from 1/v; the diagonals here are O(1), far from the
+// denormal range that .ftz flushes).
+__device__ __forceinline__ float rcp_approx(float v) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
+__device__ __forceinline__ float2 rcp_approx2(float2 v) { return make_float2(rcp_approx(v.x), rcp_approx(v.y)); }
 
 // me - me.a * L - me.c * R, normalised.
 __device__ __forceinline__ NR step_both(const NR& me, const NR& L, const NR& R) {
@@ -69,6 +77,49 @@ __device__ __forceinline__ NR step_left(const NR& me, const NR& L) {
   const float d = fmaf(-me.a, L.d, me.d);
   const float ib = rcp_approx(b);
   return {(-me.a * L.a) * ib, 0.0f, d * ib};
+}
+
+// Two rows at once (components x, y), in the paired FP32 instructions of
+// sm_100+ (one issue slot for two multiply-adds).
+struct NR2 {
+  float2 a, c, d;
+};
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+__device__ __forceinline__ NR2 step_both2(const NR2& me, const NR2& L, const NR2& R) {
+  const float2 na = neg2(me.a), nc = neg2(me.c);
+  const float2 b = __ffma2_rn(nc, R.a, __ffma2_rn(na, L.c, make_float2(1.0f, 1.0f)));
+  const float2 d = __ffma2_rn(nc, R.d, __ffma2_rn(na, L.d, me.d));
+  const float2 ib = rcp_approx2(b);
+  return {__fmul2_rn(__fmul2_rn(na, L.a), ib), __fmul2_rn(__fmul2_rn(nc, R.c), ib), __fmul2_rn(d, ib)};
+}
+__device__ __forceinline__ NR2 step_right2(const NR2& me, const NR2& R) {
+  const float2 nc = neg2(me.c);
+  const float2 b = __ffma2_rn(nc, R.a, make_float2(1.0f, 1.0f));
+  const float2 d = __ffma2_rn(nc, R.d, me.d);
+  const float2 ib = rcp_approx2(b);
+  return {make_float2(0.0f, 0.0f), __fmul2_rn(__fmul2_rn(nc, R.c), ib), __fmul2_rn(d, ib)};
+}
+__device__ __forceinline__ NR2 step_left2(const NR2& me, const NR2& L) {
+  const float2 na = neg2(me.a);
+  const float2 b = __ffma2_rn(na, L.c, make_float2(1.0f, 1.0f));
+  const float2 d = __ffma2_rn(na, L.d, me.d);
+  const float2 ib = rcp_approx2(b);
+  return {__fmul2_rn(__fmul2_rn(na, L.a), ib), make_float2(0.0f, 0.0f), __fmul2_rn(d, ib)};
+}
+__device__ __forceinline__ NR row_x(const NR2& v) { return {v.a.x, v.c.x, v.d.x}; }
+__device__ __forceinline__ NR row_y(const NR2& v) { return {v.a.y, v.c.y, v.d.y}; }
+__device__ __forceinline__ NR2 pair_of(const NR& x, const NR& y) {
+  return {make_float2(x.a, y.a), make_float2(x.c, y.c), make_float2(x.d, y.d)};
+}
+__device__ __forceinline__ NR2 shfl_up_nr2(const NR2& v, int width) {
+  return {make_float2(__shfl_up_sync(kFull, v.a.x, 1, width), __shfl_up_sync(kFull, v.a.y, 1, width)),
+          make_float2(__shfl_up_sync(kFull, v.c.x, 1, width), __shfl_up_sync(kFull, v.c.y, 1, width)),
+          make_float2(__shfl_up_sync(kFull, v.d.x, 1, width), __shfl_up_sync(kFull, v.d.y, 1, width))};
+}
+__device__ __forceinline__ NR2 shfl_down_nr2(const NR2& v, int width) {
+  return {make_float2(__shfl_down_sync(kFull, v.a.x, 1, width), __shfl_down_sync(kFull, v.a.y, 1, width)),
+          make_float2(__shfl_down_sync(kFull, v.c.x, 1, width), __shfl_down_sync(kFull, v.c.y, 1, width)),
+          make_float2(__shfl_down_sync(kFull, v.d.x, 1, width), __shfl_down_sync(kFull, v.d.y, 1, width))};
 }
 
 __device__ __forceinline__ NR shfl_up_nr(const NR& v, int width) {
@@ -141,6 +192,69 @@ __device__ __forceinline__ void phase_b_xor16(NR (&w)[kRows], int lane) {
   for (int s = 0; s < kRows; ++s) w[s] = o[s];
 }
 
+// ---- the same steps on row pairs P[j] = rows (2j, 2j+1) ----------------
+// Distance 1 (phase A) and slot distance 1 (phase B) pair a row with halves
+// of two different pairs; those steps run on single rows.
+template <int LPS>
+__device__ __forceinline__ void phase_a_step1_pairs(NR2 (&P)[kRows / 2]) {
+  const NR fromL = shfl_up_nr(row_y(P[kRows / 2 - 1]), LPS);  // previous lane's row 15
+  const NR fromR = shfl_down_nr(row_x(P[0]), LPS);            // next lane's row 0
+  NR2 o[kRows / 2];
+#pragma unroll
+  for (int j = 0; j < kRows / 2; ++j) {
+    const NR lo = step_both(row_x(P[j]), j > 0 ? row_y(P[j - 1]) : fromL, row_y(P[j]));
+    const NR hi = step_both(row_y(P[j]), row_x(P[j]), j + 1 < kRows / 2 ? row_x(P[j + 1]) : fromR);
+    o[j] = pair_of(lo, hi);
+  }
+#pragma unroll
+  for (int j = 0; j < kRows / 2; ++j) P[j] = o[j];
+}
+// Distance 2*DP rows (DP = 1, 2, 4 pairs) on contiguous rows.
+template <int DP, int LPS>
+__device__ __forceinline__ void phase_a_step_pairs(NR2 (&P)[kRows / 2]) {
+  constexpr int NP = kRows / 2;
+  NR2 o[NP];
+#pragma unroll
+  for (int j = 0; j < DP; ++j) {
+    const NR2 fromL = shfl_up_nr2(P[NP - DP + j], LPS);  // previous lane's pair NP-DP+j
+    const NR2 fromR = shfl_down_nr2(P[j], LPS);          // next lane's pair j
+#pragma unroll
+    for (int q = j; q < NP; q += DP) {
+      const NR2& L = q >= DP ? P[q - DP] : fromL;
+      const NR2& R = q + DP < NP ? P[q + DP] : fromR;
+      o[q] = step_both2(P[q], L, R);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NP; ++q) P[q] = o[q];
+}
+__device__ __forceinline__ void phase_b_step1_pairs(NR2 (&P)[kRows / 2]) {
+  NR2 o[kRows / 2];
+#pragma unroll
+  for (int j = 0; j < kRows / 2; ++j) {
+    const NR lo = j > 0 ? step_both(row_x(P[j]), row_y(P[j - 1]), row_y(P[j])) : step_right(row_x(P[j]), row_y(P[j]));
+    const NR hi = j + 1 < kRows / 2 ? step_both(row_y(P[j]), row_x(P[j]), row_x(P[j + 1]))
+                                    : step_left(row_y(P[j]), row_x(P[j]));
+    o[j] = pair_of(lo, hi);
+  }
+#pragma unroll
+  for (int j = 0; j < kRows / 2; ++j) P[j] = o[j];
+}
+// Slot distance 2*DP (DP = 1, 2 pairs).
+template <int DP>
+__device__ __forceinline__ void phase_b_step_pairs(NR2 (&P)[kRows / 2]) {
+  constexpr int NP = kRows / 2;
+  NR2 o[NP];
+#pragma unroll
+  for (int j = 0; j < NP; ++j) {
+    if (j >= DP && j + DP < NP) o[j] = step_both2(P[j], P[j - DP], P[j + DP]);
+    else if (j + DP < NP) o[j] = step_right2(P[j], P[j + DP]);
+    else o[j] = step_left2(P[j], P[j - DP]);
+  }
+#pragma unroll
+  for (int j = 0; j < NP; ++j) P[j] = o[j];
+}
+
 // Scratch index of row r of one system's word array: the rows of phase-A
 // lane p = r / 16 form a 64-byte block whose four 16-byte chunks are
 // XOR-swizzled by (p / 2) mod 4.
@@ -158,8 +272,10 @@ constexpr int kPcr2Warps = 4;
 constexpr int kPcr2TileFloats = 512;  // values of one array in a warp tile
 constexpr size_t kPcr2Smem = 128 + 1024 + (size_t)kPcr2Warps * 2 * 4 * kPcr2TileFloats * sizeof(float);
 
-// One launch: every warp streams its own tiles of 32/LPS systems.
-template <int N>
+// One launch: every warp streams its own tiles of 32/LPS systems.  PAIRED:
+// the steps whose neighbours are whole row pairs (all but distance 1 and
+// slot distance 1) run two rows per instruction (FFMA2 / FMUL2).
+template <int N, bool PAIRED>
 __global__ void __launch_bounds__(kPcr2Warps * 32, 3)
     pcr_twophase_kernel(HybridParams p, const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb,
                         const __grid_constant__ CUtensorMap mc, const __grid_constant__ CUtensorMap md) {
@@ -212,25 +328,103 @@ __global__ void __launch_bounds__(kPcr2Warps * 32, 3)
     }
     if (!mbar_wait(&bars[s], (k >> 1) & 1, p.status)) break;
     float* st = buf + s * BUF;
+    float v[4][kRows];  // a, b, c, d of the lane's 16 rows
+#pragma unroll
+    for (int arr = 0; arr < 4; ++arr)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 f = *reinterpret_cast<const float4*>(st + arr * TF + chunk[q]);
+        v[arr][4 * q] = f.x; v[arr][4 * q + 1] = f.y; v[arr][4 * q + 2] = f.z; v[arr][4 * q + 3] = f.w;
+      }
+    if (t == 0) v[0][0] = 0.0f;               // a[0] is not part of the system
+    if (t == LPS - 1) v[2][kRows - 1] = 0.0f;  // nor is c[n-1]
+    __syncwarp();  // the buffer is read: it is the transpose scratch from here on
+    float* sa = st + g * SYS_STRIDE;  // transpose scratch of this system: a, c, d words
+    float* sc = sa + N;
+    float* sd = sa + 2 * N;
+    const int rb = t * kRows;  // this lane's first phase-A row
     NR w[kRows];
-    {
-      float v[4][kRows];  // a, b, c, d of the lane's 16 rows
+    if constexpr (PAIRED) {
+      NR2 P[kRows / 2];
 #pragma unroll
-      for (int arr = 0; arr < 4; ++arr)
+      for (int j = 0; j < kRows / 2; ++j) {
+        const float2 ib = rcp_approx2(make_float2(v[1][2 * j], v[1][2 * j + 1]));
+        P[j] = NR2{__fmul2_rn(make_float2(v[0][2 * j], v[0][2 * j + 1]), ib),
+                   __fmul2_rn(make_float2(v[2][2 * j], v[2][2 * j + 1]), ib),
+                   __fmul2_rn(make_float2(v[3][2 * j], v[3][2 * j + 1]), ib)};
+      }
+      // ---- phase A: distances 1, 2, 4, 8 ----
+      phase_a_step1_pairs<LPS>(P);
+      phase_a_step_pairs<1, LPS>(P);
+      phase_a_step_pairs<2, LPS>(P);
+      phase_a_step_pairs<4, LPS>(P);
+      // ---- transpose: lane t of system g now takes rows t + LPS * s ----
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const float4 f = *reinterpret_cast<const float4*>(st + arr * TF + chunk[q]);
-          v[arr][4 * q] = f.x; v[arr][4 * q + 1] = f.y; v[arr][4 * q + 2] = f.z; v[arr][4 * q + 3] = f.w;
+      for (int q4 = 0; q4 < kRows / 4; ++q4) {
+        const int o = swz(rb + 4 * q4);
+        const NR2& u = P[2 * q4];
+        const NR2& h = P[2 * q4 + 1];
+        *reinterpret_cast<float4*>(sa + o) = make_float4(u.a.x, u.a.y, h.a.x, h.a.y);
+        *reinterpret_cast<float4*>(sc + o) = make_float4(u.c.x, u.c.y, h.c.x, h.c.y);
+        *reinterpret_cast<float4*>(sd + o) = make_float4(u.d.x, u.d.y, h.d.x, h.d.y);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < kRows / 2; ++j) {
+        const int o0 = swz(t + LPS * (2 * j)), o1 = swz(t + LPS * (2 * j + 1));
+        P[j] = NR2{make_float2(sa[o0], sa[o1]), make_float2(sc[o0], sc[o1]), make_float2(sd[o0], sd[o1])};
+      }
+      // every lane's stores and loads of the buffer are ordered before the
+      // bulk copy that refills it (issued by lane 0 after the next wait)
+      fence_proxy_async_smem();
+      __syncwarp();
+      // ---- phase B: distances 16 .. n/4 inside the lane ----
+      if constexpr (N == 512) {
+#pragma unroll
+        for (int j = 0; j < kRows / 2; ++j) { w[2 * j] = row_x(P[j]); w[2 * j + 1] = row_y(P[j]); }
+        phase_b_xor16(w, lane);
+        phase_b_step<1>(w);
+#pragma unroll
+        for (int j = 0; j < kRows / 2; ++j) P[j] = pair_of(w[2 * j], w[2 * j + 1]);
+        phase_b_step_pairs<1>(P);
+        phase_b_step_pairs<2>(P);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          const int dist = 16 << e;  // rows
+          if (dist <= N / 4) {
+            if (dist / LPS == 1) phase_b_step1_pairs(P);
+            else if (dist / LPS == 2) phase_b_step_pairs<1>(P);
+            else phase_b_step_pairs<2>(P);
+          }
         }
-      if (t == 0) v[0][0] = 0.0f;               // a[0] is not part of the system
-      if (t == LPS - 1) v[2][kRows - 1] = 0.0f;  // nor is c[n-1]
+      }
+      // ---- 2x2 systems (s, s + 8), two at a time ----
+      const long sys = tile * SPW + g;
+      if (sys < p.m) {
+        float* dst = gx + sys * N + t;
+#pragma unroll
+        for (int j = 0; j < kRows / 4; ++j) {
+          const NR2& u = P[j];
+          const NR2& l = P[j + kRows / 4];
+          const float2 den = __ffma2_rn(neg2(u.c), l.a, make_float2(1.0f, 1.0f));
+          const float2 num = __ffma2_rn(neg2(u.c), l.d, u.d);
+          const float2 xu = __fmul2_rn(num, rcp_approx2(den));
+          const float2 xl = __ffma2_rn(neg2(l.a), xu, l.d);
+          dst[LPS * (2 * j)] = xu.x;
+          dst[LPS * (2 * j + 1)] = xu.y;
+          dst[LPS * (2 * j + kRows / 2)] = xl.x;
+          dst[LPS * (2 * j + 1 + kRows / 2)] = xl.y;
+        }
+      }
+      continue;
+    } else {
 #pragma unroll
       for (int q = 0; q < kRows; ++q) {
         const float ib = rcp_approx(v[1][q]);
         w[q] = NR{v[0][q] * ib, v[2][q] * ib, v[3][q] * ib};
       }
     }
-    __syncwarp();  // the buffer is read: it is the transpose scratch from here on
 
     // ---- phase A: distances 1, 2, 4, 8 ----
     phase_a_step<1, LPS>(w);
@@ -240,10 +434,6 @@ __global__ void __launch_bounds__(kPcr2Warps * 32, 3)
 
     // ---- transpose: lane t of system g now takes rows t + LPS * s ----
     {
-      float* sa = st + g * SYS_STRIDE;
-      float* sc = sa + N;
-      float* sd = sa + 2 * N;
-      const int rb = t * kRows;  // this lane's first phase-A row
 #pragma unroll
       for (int q4 = 0; q4 < kRows / 4; ++q4) {
         const int o = swz(rb + 4 * q4);
