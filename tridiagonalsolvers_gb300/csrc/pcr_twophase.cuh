@@ -46,14 +46,6 @@ struct NR {
   float a, c, d;
 };
 
-// Reciprocal by the hardware's approximate reciprocal (PTX rcp.approx.ftz.f32:
-// at most 1 ulp from 1/v; the diagonals here are O(1), far from the
-// denormal range that .ftz flushes).
-__device__ __forceinline__ float rcp_approx(float v) {
-  float r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
-  return r;
-}
 __device__ __forceinline__ float2 rcp_approx2(float2 v) { return make_float2(rcp_approx(v.x), rcp_approx(v.y)); }
 
 // me - me.a * L - me.c * R, normalised.

@@ -11,13 +11,19 @@
 
 namespace tridi {
 
-// Division used by every solver kernel.  FP32: __fdividef, the reciprocal
-// (MUFU) times the numerator: at most 2 ulp from the IEEE quotient, no
-// slow-path branch (divisors here are O(1), far from the 2^126 limit of the
-// intrinsic).  FP64: the IEEE quotient.  Each division of the reference's
-// formulas becomes one tdiv, so results stay within a few ulp of the
-// reference's arithmetic.
-__device__ __forceinline__ float tdiv(float a, float b) { return __fdividef(a, b); }
+// Division used by every solver kernel.  FP32: the numerator times the
+// hardware's approximate reciprocal of the divisor (PTX rcp.approx.ftz.f32,
+// at most 1 ulp from 1/b; the product at most 2 ulp from the IEEE quotient),
+// no slow-path branch and no range fix-up (divisors here are O(1), far from
+// the denormal range that .ftz flushes).  FP64: the IEEE quotient.  Each
+// division of the reference's formulas becomes one tdiv, so results stay
+// within a few ulp of the reference's arithmetic.
+__device__ __forceinline__ float rcp_approx(float v) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
+__device__ __forceinline__ float tdiv(float a, float b) { return a * rcp_approx(b); }
 __device__ __forceinline__ double tdiv(double a, double b) { return a / b; }
 
 // One equation a*x[i-1] + b*x[i] + c*x[i+1] = d.
