@@ -125,38 +125,39 @@ cudaError_t launch_one(const HybridParams& p0, const DeviceInfo& dev, cudaStream
   return cudaGetLastError();
 }
 
-// FP32 PCR on 64..512 unknowns: the two-phase kernel (pcr_twophase.cuh).
-// Each array is a tensor of rows of 32 values; a warp tile is a box of 16
+// FP32 PCR on 64..1024 unknowns: the two-phase kernel (pcr_twophase.cuh).
+// Each array is a tensor of rows of 32 values; a warp tile is a box of R
 // such rows.
 template <int N, bool PAIRED>
 cudaError_t launch_pcr_twophase(const HybridParams& p, const DeviceInfo& dev, cudaStream_t stream) {
+  using S = Pcr2Shape<N>;
   auto kern = pcr_twophase_kernel<N, PAIRED>;
-  constexpr int kThreads = kPcr2Warps * 32;
+  constexpr int kThreads = S::WARPS * 32;
   const uint64_t rows = (uint64_t)p.m * N / 32;
   CUtensorMap ma, mb, mc, md;
-  if (!make_tensor_map_2d(&ma, static_cast<const float*>(p.a), 32, rows, 128, 32, kPcr2TileFloats / 32, true) ||
-      !make_tensor_map_2d(&mb, static_cast<const float*>(p.b), 32, rows, 128, 32, kPcr2TileFloats / 32, true) ||
-      !make_tensor_map_2d(&mc, static_cast<const float*>(p.c), 32, rows, 128, 32, kPcr2TileFloats / 32, true) ||
-      !make_tensor_map_2d(&md, static_cast<const float*>(p.d), 32, rows, 128, 32, kPcr2TileFloats / 32, true))
+  if (!make_tensor_map_2d(&ma, static_cast<const float*>(p.a), 32, rows, 128, 32, S::R, true) ||
+      !make_tensor_map_2d(&mb, static_cast<const float*>(p.b), 32, rows, 128, 32, S::R, true) ||
+      !make_tensor_map_2d(&mc, static_cast<const float*>(p.c), 32, rows, 128, 32, S::R, true) ||
+      !make_tensor_map_2d(&md, static_cast<const float*>(p.d), 32, rows, 128, 32, S::R, true))
     return cudaErrorInvalidValue;
-  if (kPcr2Smem > (size_t)dev.max_smem_optin) return cudaErrorInvalidConfiguration;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPcr2Smem);
+  if (S::SMEM > (size_t)dev.max_smem_optin) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, kPcr2Smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, S::SMEM);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
-  const long tiles = ((long)p.m * N + kPcr2TileFloats - 1) / kPcr2TileFloats;
+  const long tiles = ((long)p.m + S::SPW - 1) / S::SPW;
   long grid = (long)per_sm * dev.sm_count;
-  if (grid * kPcr2Warps > tiles) grid = (tiles + kPcr2Warps - 1) / kPcr2Warps;
-  kern<<<(unsigned)grid, kThreads, kPcr2Smem, stream>>>(p, ma, mb, mc, md);
+  if (grid * S::WARPS > tiles) grid = (tiles + S::WARPS - 1) / S::WARPS;
+  kern<<<(unsigned)grid, kThreads, S::SMEM, stream>>>(p, ma, mb, mc, md);
   return cudaGetLastError();
 }
 
 template <class T>
 bool pcr_twophase_applies(const HybridParams& p) {
   if constexpr (sizeof(T) != 4) return false;
-  return p.stride == 1 && (p.n == 64 || p.n == 128 || p.n == 256 || p.n == 512) && aligned16(p.a) &&
+  return p.stride == 1 && (p.n == 64 || p.n == 128 || p.n == 256 || p.n == 512 || p.n == 1024) && aligned16(p.a) &&
          aligned16(p.b) && aligned16(p.c) && aligned16(p.d) && (long)p.m * p.n / 32 < (1L << 31) &&
          tunable(TRIDI_TUNE_PCR_KERNEL) != 2;
 }
@@ -189,8 +190,10 @@ tridi_status solve_hybrid(const T* a, const T* b, const T* c, const T* d, T* x, 
                                             : launch_pcr_twophase<128, false>(p, *dev, s));
         case 256: return cuda_status(paired ? launch_pcr_twophase<256, true>(p, *dev, s)
                                             : launch_pcr_twophase<256, false>(p, *dev, s));
-        default: return cuda_status(paired ? launch_pcr_twophase<512, true>(p, *dev, s)
-                                           : launch_pcr_twophase<512, false>(p, *dev, s));
+        case 512: return cuda_status(paired ? launch_pcr_twophase<512, true>(p, *dev, s)
+                                            : launch_pcr_twophase<512, false>(p, *dev, s));
+        default: return cuda_status(paired ? launch_pcr_twophase<1024, true>(p, *dev, s)
+                                           : launch_pcr_twophase<1024, false>(p, *dev, s));
       }
     }
   }

@@ -1,4 +1,4 @@
-// Parallel cyclic reduction for FP32 systems of 64..512 unknowns in two
+// Parallel cyclic reduction for FP32 systems of 64..1024 unknowns in two
 // register phases around one transpose (replaces the device work of pcr(),
 // pcr_app.cu:5 / pcrKernel, pcr_kernel.cu:1-77, at these sizes).
 //
@@ -10,36 +10,38 @@
 // result with one reciprocal, so three words per row move between lanes and
 // each row costs one reciprocal per step.
 //
-// Mapping (n = 16 * LPS, LPS lanes per system, 32 / LPS systems per warp):
-//   phase A  lane p holds rows 16p .. 16p+15.  Steps of distance 1, 2, 4, 8
+// Mapping (R rows a lane: 16 up to n = 512, 32 at n = 1024; n = R * LPS,
+// LPS lanes per system, 32 / LPS systems per warp):
+//   phase A  lane p holds rows R p .. R p + R-1.  Steps of distance 1 .. R/2
 //            run inside the lane; a row whose neighbour lies in the next or
 //            previous lane gets it over one shuffle (3 words).
 //   transpose  the normalised rows go through the warp's staging buffer
 //            (16-byte stores, XOR-swizzled so that neither the stores nor the
 //            4-byte loads of the other side conflict on banks), and lane c
-//            takes rows c + LPS*s, s = 0 .. 15.
-//   phase B  distances 16 .. n/4 move only the slot index s (by 16/LPS ..)
-//            and stay inside the lane (n = 512: distance 16 is a lane
-//            exchange with lane c ^ 16); neighbours beyond the system's ends
-//            have coupling exactly zero and are skipped at compile time.  The
-//            closing 2x2 systems pair slots s and s+8 of the same lane.
+//            takes rows c + LPS*s, s = 0 .. R-1.
+//   phase B  distances R .. n/4 move only the slot index s and stay inside
+//            the lane (n = 512: distance 16 is a lane exchange with lane
+//            c ^ 16); neighbours beyond the system's ends have coupling
+//            exactly zero and are skipped at compile time.  The closing 2x2
+//            systems pair slots s and s + R/2 of the same lane.
 // x is written straight from phase B: for a fixed s the LPS lanes of a system
 // store LPS consecutive unknowns.
+// The steps whose neighbours are whole row pairs (rows 2j, 2j+1) -- all but
+// distance 1 and slot distance 1 -- run two rows per paired FP32 instruction
+// (FFMA2 / FMUL2, sm_100+).
 // Input rows arrive through a private two-buffer ring per warp: a tile (32/LPS
-// systems, 512 consecutive values of each array) is one 16 x 128-byte box of
+// systems, 32 R consecutive values of each array) is one R x 128-byte box of
 // each array's tensor map, copied by cp.async.bulk.tensor with the 128-byte
-// swizzle, so the 16-byte loads of a lane's 64 bytes are conflict-free with
-// no register shuffling (lane l reads box row l/2, chunks 4(l%2)+q, stored at
-// chunk (4(l%2)+q) ^ (l/2 mod 8)).  The buffer just read into registers is
-// the transpose scratch until it is refilled.
+// swizzle, so the 16-byte loads of a lane's 4 R bytes are conflict-free with
+// no register shuffling (16-byte chunk c of box row r is stored at chunk
+// c ^ (r mod 8)).  The buffer just read into registers is the transpose
+// scratch until it is refilled.
 #pragma once
 #include "tridi_device.cuh"
 
 namespace tridi {
 
 namespace pcr2 {
-
-constexpr int kRows = 16;  // rows a lane holds in either phase
 
 // One normalised row: a x[i-dl] + x[i] + c x[i+dl] = d.
 struct NR {
@@ -71,8 +73,7 @@ __device__ __forceinline__ NR step_left(const NR& me, const NR& L) {
   return {(-me.a * L.a) * ib, 0.0f, d * ib};
 }
 
-// Two rows at once (components x, y), in the paired FP32 instructions of
-// sm_100+ (one issue slot for two multiply-adds).
+// Two rows at once (components x, y).
 struct NR2 {
   float2 a, c, d;
 };
@@ -103,16 +104,6 @@ __device__ __forceinline__ NR row_y(const NR2& v) { return {v.a.y, v.c.y, v.d.y}
 __device__ __forceinline__ NR2 pair_of(const NR& x, const NR& y) {
   return {make_float2(x.a, y.a), make_float2(x.c, y.c), make_float2(x.d, y.d)};
 }
-__device__ __forceinline__ NR2 shfl_up_nr2(const NR2& v, int width) {
-  return {make_float2(__shfl_up_sync(kFull, v.a.x, 1, width), __shfl_up_sync(kFull, v.a.y, 1, width)),
-          make_float2(__shfl_up_sync(kFull, v.c.x, 1, width), __shfl_up_sync(kFull, v.c.y, 1, width)),
-          make_float2(__shfl_up_sync(kFull, v.d.x, 1, width), __shfl_up_sync(kFull, v.d.y, 1, width))};
-}
-__device__ __forceinline__ NR2 shfl_down_nr2(const NR2& v, int width) {
-  return {make_float2(__shfl_down_sync(kFull, v.a.x, 1, width), __shfl_down_sync(kFull, v.a.y, 1, width)),
-          make_float2(__shfl_down_sync(kFull, v.c.x, 1, width), __shfl_down_sync(kFull, v.c.y, 1, width)),
-          make_float2(__shfl_down_sync(kFull, v.d.x, 1, width), __shfl_down_sync(kFull, v.d.y, 1, width))};
-}
 
 __device__ __forceinline__ NR shfl_up_nr(const NR& v, int width) {
   return {__shfl_up_sync(kFull, v.a, 1, width), __shfl_up_sync(kFull, v.c, 1, width),
@@ -125,86 +116,95 @@ __device__ __forceinline__ NR shfl_down_nr(const NR& v, int width) {
 __device__ __forceinline__ NR shfl_xor_nr(const NR& v, int mask) {
   return {__shfl_xor_sync(kFull, v.a, mask), __shfl_xor_sync(kFull, v.c, mask), __shfl_xor_sync(kFull, v.d, mask)};
 }
+__device__ __forceinline__ NR2 shfl_up_nr2(const NR2& v, int width) {
+  return pair_of(shfl_up_nr(row_x(v), width), shfl_up_nr(row_y(v), width));
+}
+__device__ __forceinline__ NR2 shfl_down_nr2(const NR2& v, int width) {
+  return pair_of(shfl_down_nr(row_x(v), width), shfl_down_nr(row_y(v), width));
+}
 
-// Phase A step of distance DL (1..8) on the lane's contiguous rows.  Rows are
-// visited by residue j mod DL, so each old row dies right after its last use.
-// Lanes at the system's ends receive their own row from the shuffle: its
-// coupling there is exactly zero (a[0] = c[n-1] = 0 and, by induction over
-// the steps, every row closer to an end than the step distance).
-template <int DL, int LPS>
-__device__ __forceinline__ void phase_a_step(NR (&w)[kRows]) {
-  NR o[kRows];
+// ---- single rows ------------------------------------------------------------
+// Phase A step of distance DL (1 .. R/2) on the lane's contiguous rows.  Rows
+// are visited by residue j mod DL, so each old row dies right after its last
+// use.  Lanes at the system's ends receive their own row from the shuffle:
+// its coupling there is exactly zero (a[0] = c[n-1] = 0 and, by induction
+// over the steps, every row closer to an end than the step distance).
+template <int DL, int LPS, int R>
+__device__ __forceinline__ void phase_a_step(NR (&w)[R]) {
+  NR o[R];
 #pragma unroll
   for (int j = 0; j < DL; ++j) {
-    const NR fromL = shfl_up_nr(w[kRows - DL + j], LPS);   // previous lane's row 16-DL+j
-    const NR fromR = shfl_down_nr(w[j], LPS);              // next lane's row j
+    const NR fromL = shfl_up_nr(w[R - DL + j], LPS);  // previous lane's row R-DL+j
+    const NR fromR = shfl_down_nr(w[j], LPS);         // next lane's row j
 #pragma unroll
-    for (int q = j; q < kRows; q += DL) {
+    for (int q = j; q < R; q += DL) {
       const NR& L = q >= DL ? w[q - DL] : fromL;
-      const NR& R = q + DL < kRows ? w[q + DL] : fromR;
-      o[q] = step_both(w[q], L, R);
+      const NR& Rr = q + DL < R ? w[q + DL] : fromR;
+      o[q] = step_both(w[q], L, Rr);
     }
   }
 #pragma unroll
-  for (int q = 0; q < kRows; ++q) w[q] = o[q];
+  for (int q = 0; q < R; ++q) w[q] = o[q];
 }
 
 // Phase B step moving the slot index by K (rows c + LPS*s: distance K*LPS).
-template <int K>
-__device__ __forceinline__ void phase_b_step(NR (&w)[kRows]) {
-  NR o[kRows];
+template <int K, int R>
+__device__ __forceinline__ void phase_b_step(NR (&w)[R]) {
+  NR o[R];
 #pragma unroll
-  for (int s = 0; s < kRows; ++s) {
-    if (s >= K && s + K < kRows) o[s] = step_both(w[s], w[s - K], w[s + K]);
-    else if (s + K < kRows) o[s] = step_right(w[s], w[s + K]);
+  for (int s = 0; s < R; ++s) {
+    if (s >= K && s + K < R) o[s] = step_both(w[s], w[s - K], w[s + K]);
+    else if (s + K < R) o[s] = step_right(w[s], w[s + K]);
     else o[s] = step_left(w[s], w[s - K]);
   }
 #pragma unroll
-  for (int s = 0; s < kRows; ++s) w[s] = o[s];
+  for (int s = 0; s < R; ++s) w[s] = o[s];
 }
 
 // n = 512 only: distance 16 after the transpose (lane c holds rows c + 32 s):
 // the neighbours at +-16 are lane c ^ 16, in slot s (the nearer side) or
 // s -/+ 1 (the farther side).
-__device__ __forceinline__ void phase_b_xor16(NR (&w)[kRows], int lane) {
-  NR px[kRows];
+template <int R>
+__device__ __forceinline__ void phase_b_xor16(NR (&w)[R], int lane) {
+  NR px[R];
 #pragma unroll
-  for (int s = 0; s < kRows; ++s) px[s] = shfl_xor_nr(w[s], 16);
+  for (int s = 0; s < R; ++s) px[s] = shfl_xor_nr(w[s], 16);
   const bool lower = lane < 16;  // row c + 32 s, c < 16: R = partner slot s, L = partner slot s-1
-  NR o[kRows];
+  NR o[R];
 #pragma unroll
-  for (int s = 0; s < kRows; ++s) {
-    const NR Lf = s > 0 ? px[s - 1] : w[s];       // (beyond the first row when s = 0: coupling zero)
-    const NR Rf = s + 1 < kRows ? px[s + 1] : w[s];  // (beyond the last row)
+  for (int s = 0; s < R; ++s) {
+    const NR Lf = s > 0 ? px[s - 1] : w[s];      // (beyond the first row when s = 0: coupling zero)
+    const NR Rf = s + 1 < R ? px[s + 1] : w[s];  // (beyond the last row)
     const NR L = lower ? Lf : px[s];
-    const NR R = lower ? px[s] : Rf;
-    o[s] = step_both(w[s], L, R);
+    const NR Rr = lower ? px[s] : Rf;
+    o[s] = step_both(w[s], L, Rr);
   }
 #pragma unroll
-  for (int s = 0; s < kRows; ++s) w[s] = o[s];
+  for (int s = 0; s < R; ++s) w[s] = o[s];
 }
 
-// ---- the same steps on row pairs P[j] = rows (2j, 2j+1) ----------------
+// ---- row pairs P[j] = rows (2j, 2j+1) -------------------------------------
 // Distance 1 (phase A) and slot distance 1 (phase B) pair a row with halves
 // of two different pairs; those steps run on single rows.
-template <int LPS>
-__device__ __forceinline__ void phase_a_step1_pairs(NR2 (&P)[kRows / 2]) {
-  const NR fromL = shfl_up_nr(row_y(P[kRows / 2 - 1]), LPS);  // previous lane's row 15
-  const NR fromR = shfl_down_nr(row_x(P[0]), LPS);            // next lane's row 0
-  NR2 o[kRows / 2];
+template <int LPS, int R>
+__device__ __forceinline__ void phase_a_step1_pairs(NR2 (&P)[R / 2]) {
+  constexpr int NP = R / 2;
+  const NR fromL = shfl_up_nr(row_y(P[NP - 1]), LPS);  // previous lane's last row
+  const NR fromR = shfl_down_nr(row_x(P[0]), LPS);     // next lane's first row
+  NR2 o[NP];
 #pragma unroll
-  for (int j = 0; j < kRows / 2; ++j) {
+  for (int j = 0; j < NP; ++j) {
     const NR lo = step_both(row_x(P[j]), j > 0 ? row_y(P[j - 1]) : fromL, row_y(P[j]));
-    const NR hi = step_both(row_y(P[j]), row_x(P[j]), j + 1 < kRows / 2 ? row_x(P[j + 1]) : fromR);
+    const NR hi = step_both(row_y(P[j]), row_x(P[j]), j + 1 < NP ? row_x(P[j + 1]) : fromR);
     o[j] = pair_of(lo, hi);
   }
 #pragma unroll
-  for (int j = 0; j < kRows / 2; ++j) P[j] = o[j];
+  for (int j = 0; j < NP; ++j) P[j] = o[j];
 }
-// Distance 2*DP rows (DP = 1, 2, 4 pairs) on contiguous rows.
-template <int DP, int LPS>
-__device__ __forceinline__ void phase_a_step_pairs(NR2 (&P)[kRows / 2]) {
-  constexpr int NP = kRows / 2;
+// Distance 2*DP rows (DP whole pairs) on contiguous rows.
+template <int DP, int LPS, int R>
+__device__ __forceinline__ void phase_a_step_pairs(NR2 (&P)[R / 2]) {
+  constexpr int NP = R / 2;
   NR2 o[NP];
 #pragma unroll
   for (int j = 0; j < DP; ++j) {
@@ -213,29 +213,31 @@ __device__ __forceinline__ void phase_a_step_pairs(NR2 (&P)[kRows / 2]) {
 #pragma unroll
     for (int q = j; q < NP; q += DP) {
       const NR2& L = q >= DP ? P[q - DP] : fromL;
-      const NR2& R = q + DP < NP ? P[q + DP] : fromR;
-      o[q] = step_both2(P[q], L, R);
+      const NR2& Rr = q + DP < NP ? P[q + DP] : fromR;
+      o[q] = step_both2(P[q], L, Rr);
     }
   }
 #pragma unroll
   for (int q = 0; q < NP; ++q) P[q] = o[q];
 }
-__device__ __forceinline__ void phase_b_step1_pairs(NR2 (&P)[kRows / 2]) {
-  NR2 o[kRows / 2];
+template <int R>
+__device__ __forceinline__ void phase_b_step1_pairs(NR2 (&P)[R / 2]) {
+  constexpr int NP = R / 2;
+  NR2 o[NP];
 #pragma unroll
-  for (int j = 0; j < kRows / 2; ++j) {
+  for (int j = 0; j < NP; ++j) {
     const NR lo = j > 0 ? step_both(row_x(P[j]), row_y(P[j - 1]), row_y(P[j])) : step_right(row_x(P[j]), row_y(P[j]));
-    const NR hi = j + 1 < kRows / 2 ? step_both(row_y(P[j]), row_x(P[j]), row_x(P[j + 1]))
-                                    : step_left(row_y(P[j]), row_x(P[j]));
+    const NR hi = j + 1 < NP ? step_both(row_y(P[j]), row_x(P[j]), row_x(P[j + 1]))
+                             : step_left(row_y(P[j]), row_x(P[j]));
     o[j] = pair_of(lo, hi);
   }
 #pragma unroll
-  for (int j = 0; j < kRows / 2; ++j) P[j] = o[j];
+  for (int j = 0; j < NP; ++j) P[j] = o[j];
 }
-// Slot distance 2*DP (DP = 1, 2 pairs).
-template <int DP>
-__device__ __forceinline__ void phase_b_step_pairs(NR2 (&P)[kRows / 2]) {
-  constexpr int NP = kRows / 2;
+// Slot distance 2*DP (DP whole pairs).
+template <int DP, int R>
+__device__ __forceinline__ void phase_b_step_pairs(NR2 (&P)[R / 2]) {
+  constexpr int NP = R / 2;
   NR2 o[NP];
 #pragma unroll
   for (int j = 0; j < NP; ++j) {
@@ -247,37 +249,62 @@ __device__ __forceinline__ void phase_b_step_pairs(NR2 (&P)[kRows / 2]) {
   for (int j = 0; j < NP; ++j) P[j] = o[j];
 }
 
-// Scratch index of row r of one system's word array: the rows of phase-A
-// lane p = r / 16 form a 64-byte block whose four 16-byte chunks are
-// XOR-swizzled by (p / 2) mod 4.
+// Phase A on row pairs: distance 1, then 2 .. R/2 (whole pairs).
+template <int LPS, int R>
+__device__ __forceinline__ void phase_a_pairs(NR2 (&P)[R / 2]) {
+  phase_a_step1_pairs<LPS, R>(P);
+  phase_a_step_pairs<1, LPS, R>(P);
+  phase_a_step_pairs<2, LPS, R>(P);
+  phase_a_step_pairs<4, LPS, R>(P);
+  if constexpr (R >= 32) phase_a_step_pairs<8, LPS, R>(P);
+}
+// Phase B on row pairs, slot distance K.
+template <int K, int R>
+__device__ __forceinline__ void phase_b_pairs(NR2 (&P)[R / 2]) {
+  if constexpr (K == 1) phase_b_step1_pairs<R>(P);
+  else phase_b_step_pairs<K / 2, R>(P);
+}
+
+// Scratch index of row r of one system's word array.  The R rows of phase-A
+// lane p = r / R form a block of R/4 16-byte chunks, XOR-swizzled so that the
+// 16-byte stores of 8 consecutive lanes and the 4-byte loads of rows
+// c + LPS s (fixed s, consecutive c) each fall on distinct banks.
+template <int R>
 __device__ __forceinline__ int swz(int r) {
-  const int p = r >> 4, j = r & 15;
-  return (p << 4) + ((((j >> 2) ^ (p >> 1)) & 3) << 2) + (j & 3);
+  const int p = r / R, j = r % R;
+  if constexpr (R == 16) return (p << 4) + ((((j >> 2) ^ (p >> 1)) & 3) << 2) + (j & 3);
+  else return (p << 5) + ((((j >> 2) ^ p) & 7) << 2) + (j & 3);
 }
 
 }  // namespace pcr2
 
-// Shared memory of one CTA of kPcr2Warps warps: barriers, then (1024-byte
-// aligned, as the 128-byte swizzle requires) two ring buffers per warp of
-// 4 arrays x 2 KiB.
-constexpr int kPcr2Warps = 4;
-constexpr int kPcr2TileFloats = 512;  // values of one array in a warp tile
-constexpr size_t kPcr2Smem = 128 + 1024 + (size_t)kPcr2Warps * 2 * 4 * kPcr2TileFloats * sizeof(float);
+// Shared memory of one CTA: barriers, then (1024-byte aligned, as the
+// 128-byte swizzle requires) two ring buffers per warp of 4 arrays x 32 R
+// values; 4 warps of 2 KiB arrays (R = 16) or 2 warps of 4 KiB arrays
+// (R = 32): the same 64 KiB.
+template <int N>
+struct Pcr2Shape {
+  static constexpr int R = N >= 1024 ? 32 : 16;  // rows a lane holds
+  static constexpr int LPS = N / R;              // lanes per system
+  static constexpr int SPW = 32 / LPS;           // systems per warp tile
+  static constexpr int TF = 32 * R;              // values of one array in a warp tile (= SPW * N)
+  static constexpr int WARPS = R == 32 ? 2 : 4;  // warps per CTA
+  static constexpr size_t SMEM = 128 + 1024 + (size_t)WARPS * 2 * 4 * TF * sizeof(float);
+};
 
 // One launch: every warp streams its own tiles of 32/LPS systems.  PAIRED:
-// the steps whose neighbours are whole row pairs (all but distance 1 and
-// slot distance 1) run two rows per instruction (FFMA2 / FMUL2).
+// the steps whose neighbours are whole row pairs run two rows per
+// instruction; otherwise every step runs on single rows.
 template <int N, bool PAIRED>
-__global__ void __launch_bounds__(kPcr2Warps * 32, 3)
+__global__ void __launch_bounds__(Pcr2Shape<N>::WARPS * 32, 3)
     pcr_twophase_kernel(HybridParams p, const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb,
                         const __grid_constant__ CUtensorMap mc, const __grid_constant__ CUtensorMap md) {
   using namespace pcr2;
-  constexpr int LPS = N / kRows;  // lanes per system
-  constexpr int SPW = 32 / LPS;   // systems per warp tile
-  constexpr int TF = kPcr2TileFloats;  // = SPW * N
-  constexpr int BUF = 4 * TF;          // floats per ring buffer (a, b, c, d of a tile)
+  using S = Pcr2Shape<N>;
+  constexpr int R = S::R, LPS = S::LPS, SPW = S::SPW, TF = S::TF;
+  constexpr int BUF = 4 * TF;              // floats per ring buffer (a, b, c, d of a tile)
   constexpr int SYS_STRIDE = 3 * N + LPS;  // transpose scratch per system (padded: no bank conflicts)
-  static_assert(N >= 64 && N <= 512 && SPW * N == TF && SPW * SYS_STRIDE <= BUF, "pcr_twophase: 64 <= n <= 512");
+  static_assert(N >= 64 && N <= 1024 && SPW * N == TF && SPW * SYS_STRIDE <= BUF, "pcr_twophase: 64 <= n <= 1024");
   extern __shared__ __align__(128) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + 2 * warp;
@@ -305,10 +332,13 @@ __global__ void __launch_bounds__(kPcr2Warps * 32, 3)
   };
   if (lane == 0 && first < tiles) issue(first, 0);
   const int g = lane / LPS, t = lane % LPS;
-  // this lane's four swizzled 16-byte chunks in a box (row lane/2)
-  int chunk[4];
+  // this lane's R/4 swizzled 16-byte chunks in a box: chunk index lane*R/4 + q
+  int chunk[R / 4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) chunk[q] = (lane >> 1) * 32 + ((((lane & 1) * 4 + q) ^ ((lane >> 1) & 7)) << 2);
+  for (int q = 0; q < R / 4; ++q) {
+    const int c = lane * (R / 4) + q, row = c >> 3;
+    chunk[q] = row * 32 + (((c & 7) ^ (row & 7)) << 2);
+  }
   int k = 0;
   for (long tile = first; tile < tiles; tile += step, ++k) {
     const int s = k & 1;
@@ -320,40 +350,37 @@ __global__ void __launch_bounds__(kPcr2Warps * 32, 3)
     }
     if (!mbar_wait(&bars[s], (k >> 1) & 1, p.status)) break;
     float* st = buf + s * BUF;
-    float v[4][kRows];  // a, b, c, d of the lane's 16 rows
+    float v[4][R];  // a, b, c, d of the lane's R rows
 #pragma unroll
     for (int arr = 0; arr < 4; ++arr)
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < R / 4; ++q) {
         const float4 f = *reinterpret_cast<const float4*>(st + arr * TF + chunk[q]);
         v[arr][4 * q] = f.x; v[arr][4 * q + 1] = f.y; v[arr][4 * q + 2] = f.z; v[arr][4 * q + 3] = f.w;
       }
-    if (t == 0) v[0][0] = 0.0f;               // a[0] is not part of the system
-    if (t == LPS - 1) v[2][kRows - 1] = 0.0f;  // nor is c[n-1]
+    if (t == 0) v[0][0] = 0.0f;            // a[0] is not part of the system
+    if (t == LPS - 1) v[2][R - 1] = 0.0f;  // nor is c[n-1]
     __syncwarp();  // the buffer is read: it is the transpose scratch from here on
     float* sa = st + g * SYS_STRIDE;  // transpose scratch of this system: a, c, d words
     float* sc = sa + N;
     float* sd = sa + 2 * N;
-    const int rb = t * kRows;  // this lane's first phase-A row
-    NR w[kRows];
+    const int rb = t * R;  // this lane's first phase-A row
+    const long sys = tile * SPW + g;
+    float* dst = gx + sys * N + t;
     if constexpr (PAIRED) {
-      NR2 P[kRows / 2];
+      NR2 P[R / 2];
 #pragma unroll
-      for (int j = 0; j < kRows / 2; ++j) {
+      for (int j = 0; j < R / 2; ++j) {
         const float2 ib = rcp_approx2(make_float2(v[1][2 * j], v[1][2 * j + 1]));
         P[j] = NR2{__fmul2_rn(make_float2(v[0][2 * j], v[0][2 * j + 1]), ib),
                    __fmul2_rn(make_float2(v[2][2 * j], v[2][2 * j + 1]), ib),
                    __fmul2_rn(make_float2(v[3][2 * j], v[3][2 * j + 1]), ib)};
       }
-      // ---- phase A: distances 1, 2, 4, 8 ----
-      phase_a_step1_pairs<LPS>(P);
-      phase_a_step_pairs<1, LPS>(P);
-      phase_a_step_pairs<2, LPS>(P);
-      phase_a_step_pairs<4, LPS>(P);
+      phase_a_pairs<LPS, R>(P);
       // ---- transpose: lane t of system g now takes rows t + LPS * s ----
 #pragma unroll
-      for (int q4 = 0; q4 < kRows / 4; ++q4) {
-        const int o = swz(rb + 4 * q4);
+      for (int q4 = 0; q4 < R / 4; ++q4) {
+        const int o = swz<R>(rb + 4 * q4);
         const NR2& u = P[2 * q4];
         const NR2& h = P[2 * q4 + 1];
         *reinterpret_cast<float4*>(sa + o) = make_float4(u.a.x, u.a.y, h.a.x, h.a.y);
@@ -362,119 +389,101 @@ __global__ void __launch_bounds__(kPcr2Warps * 32, 3)
       }
       __syncwarp();
 #pragma unroll
-      for (int j = 0; j < kRows / 2; ++j) {
-        const int o0 = swz(t + LPS * (2 * j)), o1 = swz(t + LPS * (2 * j + 1));
+      for (int j = 0; j < R / 2; ++j) {
+        const int o0 = swz<R>(t + LPS * (2 * j)), o1 = swz<R>(t + LPS * (2 * j + 1));
         P[j] = NR2{make_float2(sa[o0], sa[o1]), make_float2(sc[o0], sc[o1]), make_float2(sd[o0], sd[o1])};
       }
       // every lane's stores and loads of the buffer are ordered before the
       // bulk copy that refills it (issued by lane 0 after the next wait)
       fence_proxy_async_smem();
       __syncwarp();
-      // ---- phase B: distances 16 .. n/4 inside the lane ----
+      // ---- phase B: distances R .. n/4 ----
       if constexpr (N == 512) {
+        NR w[R];
 #pragma unroll
-        for (int j = 0; j < kRows / 2; ++j) { w[2 * j] = row_x(P[j]); w[2 * j + 1] = row_y(P[j]); }
-        phase_b_xor16(w, lane);
-        phase_b_step<1>(w);
-#pragma unroll
-        for (int j = 0; j < kRows / 2; ++j) P[j] = pair_of(w[2 * j], w[2 * j + 1]);
-        phase_b_step_pairs<1>(P);
-        phase_b_step_pairs<2>(P);
-      } else {
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
-          const int dist = 16 << e;  // rows
-          if (dist <= N / 4) {
-            if (dist / LPS == 1) phase_b_step1_pairs(P);
-            else if (dist / LPS == 2) phase_b_step_pairs<1>(P);
-            else phase_b_step_pairs<2>(P);
-          }
+        for (int j = 0; j < R / 2; ++j) {
+          w[2 * j] = row_x(P[j]);
+          w[2 * j + 1] = row_y(P[j]);
         }
-      }
-      // ---- 2x2 systems (s, s + 8), two at a time ----
-      const long sys = tile * SPW + g;
-      if (sys < p.m) {
-        float* dst = gx + sys * N + t;
+        phase_b_xor16<R>(w, lane);
+        phase_b_step<1, R>(w);
 #pragma unroll
-        for (int j = 0; j < kRows / 4; ++j) {
+        for (int j = 0; j < R / 2; ++j) P[j] = pair_of(w[2 * j], w[2 * j + 1]);
+        phase_b_pairs<2, R>(P);
+        phase_b_pairs<4, R>(P);
+      } else {
+        if constexpr (R <= N / 4) phase_b_pairs<R / LPS, R>(P);
+        if constexpr (2 * R <= N / 4) phase_b_pairs<2 * R / LPS, R>(P);
+        if constexpr (4 * R <= N / 4) phase_b_pairs<4 * R / LPS, R>(P);
+        if constexpr (8 * R <= N / 4) phase_b_pairs<8 * R / LPS, R>(P);
+      }
+      // ---- 2x2 systems (s, s + R/2), two at a time ----
+      if (sys < p.m) {
+#pragma unroll
+        for (int j = 0; j < R / 4; ++j) {
           const NR2& u = P[j];
-          const NR2& l = P[j + kRows / 4];
+          const NR2& l = P[j + R / 4];
           const float2 den = __ffma2_rn(neg2(u.c), l.a, make_float2(1.0f, 1.0f));
           const float2 num = __ffma2_rn(neg2(u.c), l.d, u.d);
           const float2 xu = __fmul2_rn(num, rcp_approx2(den));
           const float2 xl = __ffma2_rn(neg2(l.a), xu, l.d);
           dst[LPS * (2 * j)] = xu.x;
           dst[LPS * (2 * j + 1)] = xu.y;
-          dst[LPS * (2 * j + kRows / 2)] = xl.x;
-          dst[LPS * (2 * j + 1 + kRows / 2)] = xl.y;
+          dst[LPS * (2 * j + R / 2)] = xl.x;
+          dst[LPS * (2 * j + 1 + R / 2)] = xl.y;
         }
       }
-      continue;
     } else {
+      NR w[R];
 #pragma unroll
-      for (int q = 0; q < kRows; ++q) {
+      for (int q = 0; q < R; ++q) {
         const float ib = rcp_approx(v[1][q]);
         w[q] = NR{v[0][q] * ib, v[2][q] * ib, v[3][q] * ib};
       }
-    }
-
-    // ---- phase A: distances 1, 2, 4, 8 ----
-    phase_a_step<1, LPS>(w);
-    phase_a_step<2, LPS>(w);
-    phase_a_step<4, LPS>(w);
-    phase_a_step<8, LPS>(w);
-
-    // ---- transpose: lane t of system g now takes rows t + LPS * s ----
-    {
+      phase_a_step<1, LPS, R>(w);
+      phase_a_step<2, LPS, R>(w);
+      phase_a_step<4, LPS, R>(w);
+      phase_a_step<8, LPS, R>(w);
+      if constexpr (R >= 32) phase_a_step<16, LPS, R>(w);
+      // ---- transpose ----
 #pragma unroll
-      for (int q4 = 0; q4 < kRows / 4; ++q4) {
-        const int o = swz(rb + 4 * q4);
+      for (int q4 = 0; q4 < R / 4; ++q4) {
+        const int o = swz<R>(rb + 4 * q4);
         *reinterpret_cast<float4*>(sa + o) = make_float4(w[4 * q4].a, w[4 * q4 + 1].a, w[4 * q4 + 2].a, w[4 * q4 + 3].a);
         *reinterpret_cast<float4*>(sc + o) = make_float4(w[4 * q4].c, w[4 * q4 + 1].c, w[4 * q4 + 2].c, w[4 * q4 + 3].c);
         *reinterpret_cast<float4*>(sd + o) = make_float4(w[4 * q4].d, w[4 * q4 + 1].d, w[4 * q4 + 2].d, w[4 * q4 + 3].d);
       }
       __syncwarp();
 #pragma unroll
-      for (int q = 0; q < kRows; ++q) {
-        const int o = swz(t + LPS * q);
+      for (int q = 0; q < R; ++q) {
+        const int o = swz<R>(t + LPS * q);
         w[q] = NR{sa[o], sc[o], sd[o]};
       }
-      // every lane's stores and loads of the buffer are ordered before the
-      // bulk copy that refills it (issued by lane 0 after the next wait)
       fence_proxy_async_smem();
       __syncwarp();
-    }
-
-    // ---- phase B: distances 16 .. n/4 inside the lane ----
-    if constexpr (N == 512) {
-      phase_b_xor16(w, lane);
-      phase_b_step<1>(w);
-      phase_b_step<2>(w);
-      phase_b_step<4>(w);
-    } else {
-#pragma unroll
-      for (int e = 0; e < 3; ++e) {
-        const int dist = 16 << e;  // rows
-        if (dist <= N / 4) {
-          if (dist / LPS == 1) phase_b_step<1>(w);
-          else if (dist / LPS == 2) phase_b_step<2>(w);
-          else phase_b_step<4>(w);
-        }
+      // ---- phase B ----
+      if constexpr (N == 512) {
+        phase_b_xor16<R>(w, lane);
+        phase_b_step<1, R>(w);
+        phase_b_step<2, R>(w);
+        phase_b_step<4, R>(w);
+      } else {
+        if constexpr (R <= N / 4) phase_b_step<R / LPS, R>(w);
+        if constexpr (2 * R <= N / 4) phase_b_step<2 * R / LPS, R>(w);
+        if constexpr (4 * R <= N / 4) phase_b_step<4 * R / LPS, R>(w);
+        if constexpr (8 * R <= N / 4) phase_b_step<8 * R / LPS, R>(w);
       }
-    }
-
-    // ---- 2x2 systems (s, s + 8): x_u + c_u x_l = d_u, a_l x_u + x_l = d_l ----
-    const long sys = tile * SPW + g;
-    if (sys < p.m) {
-      float* dst = gx + sys * N + t;
+      // ---- 2x2 systems (s, s + R/2): x_u + c_u x_l = d_u, a_l x_u + x_l = d_l ----
+      if (sys < p.m) {
 #pragma unroll
-      for (int q = 0; q < kRows / 2; ++q) {
-        const NR& u = w[q];
-        const NR& l = w[q + kRows / 2];
-        const float xu = (u.d - u.c * l.d) * rcp_approx(fmaf(-u.c, l.a, 1.0f));
-        const float xl = fmaf(-l.a, xu, l.d);
-        dst[LPS * q] = xu;
-        dst[LPS * (q + kRows / 2)] = xl;
+        for (int q = 0; q < R / 2; ++q) {
+          const NR& u = w[q];
+          const NR& l = w[q + R / 2];
+          const float xu = (u.d - u.c * l.d) * rcp_approx(fmaf(-u.c, l.a, 1.0f));
+          const float xl = fmaf(-l.a, xu, l.d);
+          dst[LPS * q] = xu;
+          dst[LPS * (q + R / 2)] = xl;
+        }
       }
     }
   }
