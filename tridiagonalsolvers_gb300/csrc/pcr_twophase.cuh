@@ -29,13 +29,15 @@
 // The steps whose neighbours are whole row pairs (rows 2j, 2j+1) -- all but
 // distance 1 and slot distance 1 -- run two rows per paired FP32 instruction
 // (FFMA2 / FMUL2, sm_100+).
-// Input rows arrive through a private two-buffer ring per warp: a tile (32/LPS
+// Input rows arrive through one staging buffer per warp: a tile (32/LPS
 // systems, 32 R consecutive values of each array) is one R x 128-byte box of
 // each array's tensor map, copied by cp.async.bulk.tensor with the 128-byte
 // swizzle, so the 16-byte loads of a lane's 4 R bytes are conflict-free with
 // no register shuffling (16-byte chunk c of box row r is stored at chunk
-// c ^ (r mod 8)).  The buffer just read into registers is the transpose
-// scratch until it is refilled.
+// c ^ (r mod 8)).  As soon as a tile is in registers the warp issues the
+// next one into the same buffer: its load has the whole solve of this tile
+// to land, and one buffer per warp (plus a transpose scratch of one word
+// array) lets more warps share an SM.
 #pragma once
 #include "tridi_device.cuh"
 
@@ -276,12 +278,30 @@ __device__ __forceinline__ int swz(int r) {
   else return (p << 5) + ((((j >> 2) ^ p) & 7) << 2) + (j & 3);
 }
 
+// One word array of the transpose through the warp's scratch: the lane's
+// phase-A rows rb .. rb+R-1 go out as 16-byte stores, rows t + LPS*s come
+// back (word(j) is the pair of rows 2j, 2j+1 before and slots 2j, 2j+1
+// after).  The warp synchronises before the loads and after them (the next
+// word array reuses the scratch).
+template <int R, int LPS, class Word>
+__device__ __forceinline__ void transpose_word(float* sw, int rb, int t, Word word) {
+#pragma unroll
+  for (int q4 = 0; q4 < R / 4; ++q4) {
+    const float2 u = word(2 * q4), h = word(2 * q4 + 1);
+    *reinterpret_cast<float4*>(sw + swz<R>(rb + 4 * q4)) = make_float4(u.x, u.y, h.x, h.y);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < R / 2; ++j) word(j) = make_float2(sw[swz<R>(t + LPS * (2 * j))], sw[swz<R>(t + LPS * (2 * j + 1))]);
+  __syncwarp();
+}
+
 }  // namespace pcr2
 
-// Shared memory of one CTA: barriers, then (1024-byte aligned, as the
-// 128-byte swizzle requires) two ring buffers per warp of 4 arrays x 32 R
-// values; 4 warps of 2 KiB arrays (R = 16) or 2 warps of 4 KiB arrays
-// (R = 32): the same 64 KiB.
+// Shared memory of one CTA: barriers, the transpose scratch of every warp
+// (one word array of its tile, padded per system), then (1024-byte aligned,
+// as the 128-byte swizzle requires) one staging buffer per warp of 4 arrays
+// x 32 R values.
 template <int N>
 struct Pcr2Shape {
   static constexpr int R = N >= 1024 ? 32 : 16;  // rows a lane holds
@@ -289,7 +309,10 @@ struct Pcr2Shape {
   static constexpr int SPW = 32 / LPS;           // systems per warp tile
   static constexpr int TF = 32 * R;              // values of one array in a warp tile (= SPW * N)
   static constexpr int WARPS = R == 32 ? 2 : 4;  // warps per CTA
-  static constexpr size_t SMEM = 128 + 1024 + (size_t)WARPS * 2 * 4 * TF * sizeof(float);
+  static constexpr int SYS_STRIDE = N + LPS;     // transpose scratch per system (padded: no bank conflicts)
+  static constexpr int SCRATCH = SPW * SYS_STRIDE;  // floats per warp
+  static constexpr size_t SMEM = 128 + (size_t)WARPS * SCRATCH * sizeof(float) + 1024 +
+                                 (size_t)WARPS * 4 * TF * sizeof(float);
 };
 
 // One launch: every warp streams its own tiles of 32/LPS systems.  PAIRED:
@@ -302,35 +325,34 @@ __global__ void __launch_bounds__(Pcr2Shape<N>::WARPS * 32, 3)
   using namespace pcr2;
   using S = Pcr2Shape<N>;
   constexpr int R = S::R, LPS = S::LPS, SPW = S::SPW, TF = S::TF;
-  constexpr int BUF = 4 * TF;              // floats per ring buffer (a, b, c, d of a tile)
-  constexpr int SYS_STRIDE = 3 * N + LPS;  // transpose scratch per system (padded: no bank conflicts)
-  static_assert(N >= 64 && N <= 1024 && SPW * N == TF && SPW * SYS_STRIDE <= BUF, "pcr_twophase: 64 <= n <= 1024");
+  constexpr int BUF = 4 * TF;  // floats per staging buffer (a, b, c, d of a tile)
+  constexpr int SYS_STRIDE = S::SYS_STRIDE;
+  static_assert(N >= 64 && N <= 1024 && SPW * N == TF, "pcr_twophase: 64 <= n <= 1024");
   extern __shared__ __align__(128) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + 2 * warp;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem) + warp;
+  float* scratch = reinterpret_cast<float*>(smem + 128) + (size_t)warp * S::SCRATCH;
   const uint32_t base = smem_addr(smem);
-  const uint32_t ring = (base + 128 + 1023) & ~1023u;
-  float* buf = reinterpret_cast<float*>(smem + (ring - base)) + (size_t)2 * warp * BUF;
+  const uint32_t ring = (base + 128 + S::WARPS * S::SCRATCH * (uint32_t)sizeof(float) + 1023) & ~1023u;
+  float* buf = reinterpret_cast<float*>(smem + (ring - base)) + (size_t)warp * BUF;
   float* gx = static_cast<float*>(p.x);
   const long tiles = ((long)p.m + SPW - 1) / SPW;
   const long first = (long)blockIdx.x * (blockDim.x >> 5) + warp;
   const long step = (long)gridDim.x * (blockDim.x >> 5);
   if (lane == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
+    mbar_init(bar, 1);
     mbar_fence_init();
   }
   __syncwarp();
-  const auto issue = [&](long tile, int s) {  // lane 0; the last tile's box reads zeros beyond the batch
-    float* st = buf + s * BUF;
+  const auto issue = [&](long tile) {  // lane 0; the last tile's box reads zeros beyond the batch
     const int row = (int)(tile * (TF / 32));
-    mbar_arrive_expect_tx(&bars[s], 4 * TF * sizeof(float));
-    tma_load_2d(st + 0 * TF, &ma, 0, row, &bars[s]);
-    tma_load_2d(st + 1 * TF, &mb, 0, row, &bars[s]);
-    tma_load_2d(st + 2 * TF, &mc, 0, row, &bars[s]);
-    tma_load_2d(st + 3 * TF, &md, 0, row, &bars[s]);
+    mbar_arrive_expect_tx(bar, 4 * TF * sizeof(float));
+    tma_load_2d(buf + 0 * TF, &ma, 0, row, bar);
+    tma_load_2d(buf + 1 * TF, &mb, 0, row, bar);
+    tma_load_2d(buf + 2 * TF, &mc, 0, row, bar);
+    tma_load_2d(buf + 3 * TF, &md, 0, row, bar);
   };
-  if (lane == 0 && first < tiles) issue(first, 0);
+  if (lane == 0 && first < tiles) issue(first);
   const int g = lane / LPS, t = lane % LPS;
   // this lane's R/4 swizzled 16-byte chunks in a box: chunk index lane*R/4 + q
   int chunk[R / 4];
@@ -341,29 +363,23 @@ __global__ void __launch_bounds__(Pcr2Shape<N>::WARPS * 32, 3)
   }
   int k = 0;
   for (long tile = first; tile < tiles; tile += step, ++k) {
-    const int s = k & 1;
-    // the other buffer was last used (transpose scratch) one tile ago and
-    // the warp synchronised since: refill it with the next tile
-    if (lane == 0 && tile + step < tiles) {
-      fence_proxy_async_smem();
-      issue(tile + step, s ^ 1);
-    }
-    if (!mbar_wait(&bars[s], (k >> 1) & 1, p.status)) break;
-    float* st = buf + s * BUF;
+    if (!mbar_wait(bar, k & 1, p.status)) break;
     float v[4][R];  // a, b, c, d of the lane's R rows
 #pragma unroll
     for (int arr = 0; arr < 4; ++arr)
 #pragma unroll
       for (int q = 0; q < R / 4; ++q) {
-        const float4 f = *reinterpret_cast<const float4*>(st + arr * TF + chunk[q]);
+        const float4 f = *reinterpret_cast<const float4*>(buf + arr * TF + chunk[q]);
         v[arr][4 * q] = f.x; v[arr][4 * q + 1] = f.y; v[arr][4 * q + 2] = f.z; v[arr][4 * q + 3] = f.w;
       }
+    // every lane's loads of the buffer are ordered before the bulk copies
+    // that refill it with the next tile
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0 && tile + step < tiles) issue(tile + step);
     if (t == 0) v[0][0] = 0.0f;            // a[0] is not part of the system
     if (t == LPS - 1) v[2][R - 1] = 0.0f;  // nor is c[n-1]
-    __syncwarp();  // the buffer is read: it is the transpose scratch from here on
-    float* sa = st + g * SYS_STRIDE;  // transpose scratch of this system: a, c, d words
-    float* sc = sa + N;
-    float* sd = sa + 2 * N;
+    float* sw = scratch + g * SYS_STRIDE;  // this system's transpose scratch (one word array)
     const int rb = t * R;  // this lane's first phase-A row
     const long sys = tile * SPW + g;
     float* dst = gx + sys * N + t;
@@ -377,26 +393,11 @@ __global__ void __launch_bounds__(Pcr2Shape<N>::WARPS * 32, 3)
                    __fmul2_rn(make_float2(v[3][2 * j], v[3][2 * j + 1]), ib)};
       }
       phase_a_pairs<LPS, R>(P);
-      // ---- transpose: lane t of system g now takes rows t + LPS * s ----
-#pragma unroll
-      for (int q4 = 0; q4 < R / 4; ++q4) {
-        const int o = swz<R>(rb + 4 * q4);
-        const NR2& u = P[2 * q4];
-        const NR2& h = P[2 * q4 + 1];
-        *reinterpret_cast<float4*>(sa + o) = make_float4(u.a.x, u.a.y, h.a.x, h.a.y);
-        *reinterpret_cast<float4*>(sc + o) = make_float4(u.c.x, u.c.y, h.c.x, h.c.y);
-        *reinterpret_cast<float4*>(sd + o) = make_float4(u.d.x, u.d.y, h.d.x, h.d.y);
-      }
-      __syncwarp();
-#pragma unroll
-      for (int j = 0; j < R / 2; ++j) {
-        const int o0 = swz<R>(t + LPS * (2 * j)), o1 = swz<R>(t + LPS * (2 * j + 1));
-        P[j] = NR2{make_float2(sa[o0], sa[o1]), make_float2(sc[o0], sc[o1]), make_float2(sd[o0], sd[o1])};
-      }
-      // every lane's stores and loads of the buffer are ordered before the
-      // bulk copy that refills it (issued by lane 0 after the next wait)
-      fence_proxy_async_smem();
-      __syncwarp();
+      // ---- transpose, one word array at a time: lane t of system g now
+      //      takes rows t + LPS * s ----
+      transpose_word<R, LPS>(sw, rb, t, [&](int j) -> float2& { return P[j].a; });
+      transpose_word<R, LPS>(sw, rb, t, [&](int j) -> float2& { return P[j].c; });
+      transpose_word<R, LPS>(sw, rb, t, [&](int j) -> float2& { return P[j].d; });
       // ---- phase B: distances R .. n/4 ----
       if constexpr (N == 512) {
         NR w[R];
@@ -446,21 +447,19 @@ __global__ void __launch_bounds__(Pcr2Shape<N>::WARPS * 32, 3)
       phase_a_step<8, LPS, R>(w);
       if constexpr (R >= 32) phase_a_step<16, LPS, R>(w);
       // ---- transpose ----
+      {
+        NR2 P[R / 2];
 #pragma unroll
-      for (int q4 = 0; q4 < R / 4; ++q4) {
-        const int o = swz<R>(rb + 4 * q4);
-        *reinterpret_cast<float4*>(sa + o) = make_float4(w[4 * q4].a, w[4 * q4 + 1].a, w[4 * q4 + 2].a, w[4 * q4 + 3].a);
-        *reinterpret_cast<float4*>(sc + o) = make_float4(w[4 * q4].c, w[4 * q4 + 1].c, w[4 * q4 + 2].c, w[4 * q4 + 3].c);
-        *reinterpret_cast<float4*>(sd + o) = make_float4(w[4 * q4].d, w[4 * q4 + 1].d, w[4 * q4 + 2].d, w[4 * q4 + 3].d);
-      }
-      __syncwarp();
+        for (int j = 0; j < R / 2; ++j) P[j] = pair_of(w[2 * j], w[2 * j + 1]);
+        transpose_word<R, LPS>(sw, rb, t, [&](int j) -> float2& { return P[j].a; });
+        transpose_word<R, LPS>(sw, rb, t, [&](int j) -> float2& { return P[j].c; });
+        transpose_word<R, LPS>(sw, rb, t, [&](int j) -> float2& { return P[j].d; });
 #pragma unroll
-      for (int q = 0; q < R; ++q) {
-        const int o = swz<R>(t + LPS * q);
-        w[q] = NR{sa[o], sc[o], sd[o]};
+        for (int j = 0; j < R / 2; ++j) {
+          w[2 * j] = row_x(P[j]);
+          w[2 * j + 1] = row_y(P[j]);
+        }
       }
-      fence_proxy_async_smem();
-      __syncwarp();
       // ---- phase B ----
       if constexpr (N == 512) {
         phase_b_xor16<R>(w, lane);
