@@ -317,6 +317,9 @@ tridi_status tridi_selfcheck_wait(long long limit_cycles, int arrive, int *timed
    TRIDI_ERROR_WORKSPACE_TOO_SMALL.  The array is shared by all calls on a
    device: calls that overlap on the GPU race on it.  The first call on a
    device looks up the array's address; make it before any stream capture.
+   The address is kept for the life of the process: after a device reset
+   (cudaDeviceReset, which unloads the library's module) it is stale, so do
+   not call this entry point again in a process that reset the device.
    CUDA errors are reported by tridi_noalloc_last_cuda_error(). */
 long tridi_noalloc_max_unknowns(void);
 int tridi_noalloc_last_cuda_error(void);
