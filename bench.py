@@ -18,6 +18,7 @@ Lines printed (rank 0, one JSON line):
     over its switch levels) for the same batch.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py --workload kernel --kernel pcr --system-size 256 --num-systems 65536 [--param P]
 
 --impl reference times the reference's own CPU gold solver (the oracle's
 restatement of tridiagonal_gold.h, bit-identical to it) on every host core,
@@ -808,6 +809,74 @@ def run_serve(args):
     return 0
 
 
+KERNELS = ("cr", "pcr", "crpcr", "crNBC", "crNBC32", "crpcrNBC", "pcrGauss", "partition", "large", "refine")
+
+
+def run_kernel(args):
+    """One solver of the family on one seeded batch (`--kernel`, `--system-size`,
+    `--num-systems`, `--param` = rest / gaussian, `--tunable KEY=VALUE`):
+    W untimed and K timed launches back to back on one stream, CUDA events.
+    Strictly diagonally dominant inputs (weakly dominant and interleaved for
+    large / refine).  Also the command that ncu captures of one kernel run."""
+    import torch
+
+    from tridiagonalsolvers_gb300 import _lib, solvers, workloads
+
+    lib = _lib.lib()
+    for kv in args.tunable:
+        key, val = (int(v) for v in kv.split("="))
+        _lib.check(lib.tridi_set_tunable(key, val), "tridi_set_tunable")
+    dev = torch.device("cuda", 0)
+    n, m, kind = args.system_size, args.num_systems, args.kernel
+    inter = kind in ("large", "refine")
+    gen = workloads.weak if inter else workloads.dominant
+    a, b, c, d = gen(m, n, seed=workloads.SEEDS["c2"], layout=1 if inter else 0)
+    t = [torch.from_numpy(v).to(dev).reshape(-1) for v in (a, b, c, d)]
+    x = torch.empty_like(t[0])
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    ptrs = [v.data_ptr() for v in (*t, x)]
+    param = args.param
+    direct = {
+        "cr": lambda: lib.tridi_cr_f32(*ptrs, n, m, sp), "pcr": lambda: lib.tridi_pcr_f32(*ptrs, n, m, sp),
+        "crpcr": lambda: lib.tridi_crpcr_f32(*ptrs, n, m, param or 32, sp),
+        "crNBC": lambda: lib.tridi_cr_nbc_f32(*ptrs, n, m, sp), "crNBC32": lambda: lib.tridi_cr_nbc_f32(*ptrs, n, m, sp),
+        "crpcrNBC": lambda: lib.tridi_crpcr_nbc_f32(*ptrs, n, m, param or 32, sp),
+        "pcrGauss": lambda: lib.tridi_pcr_thomas_f32(*ptrs, n, m, param, sp),
+        "partition": lambda: lib.tridi_solve_f32(*ptrs, n, m, sp),
+    }
+    if kind in direct:
+        def step():
+            _lib.check(direct[kind](), kind)
+    elif kind == "large":
+        wsb = lib.tridi_large_workspace_bytes(n, m, 4)
+        ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+
+        def step():
+            _lib.check(lib.tridi_solve_large_f32(*ptrs, n, m, 1, ws.data_ptr(), wsb, sp), "tridi_solve_large_f32")
+    else:
+        x64 = torch.empty(n * m, dtype=torch.float64, device=dev)
+
+        def step():
+            solvers.refine(*t, n, m, layout="interleaved", tol=1e-10, max_sweeps=20, x=x64)
+    with ClockSampler(0) as clk:
+        ms = time_kernel(step, stream, args.warmup, args.steps)
+    peak, peak_kind = measured_peaks()
+    bpu = 24 if kind == "refine" else BYTES_PER_UNKNOWN
+    gbs = bpu * n * m / (ms * 1e-3) / 1e9
+    line = {"metric": METRIC, "value": n * m / (ms * 1e-3), "unit": "unknowns/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{kind}, {m} systems x {n} unknowns" + (", interleaved" if inter else ""),
+                       "param": param, "tunables": args.tunable, "seed": workloads.SEEDS["c2"],
+                       "l2": "back-to-back launches"},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "peak_source": peak_kind, "bytes_per_unknown": bpu},
+            "clocks": clk.summary(), "device_status": solvers.device_status()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def workloads_seed(tag):
     from tridiagonalsolvers_gb300 import workloads
 
@@ -824,9 +893,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-reference-kernels", action="store_true",
                     help="per-kernel tables without the reference's own kernels beside them")
-    ap.add_argument("--workload", default="batch", choices=["batch", "large", "ragged", "serve"],
+    ap.add_argument("--workload", default="batch", choices=["batch", "large", "ragged", "serve", "kernel"],
                     help="batch: 65536 x 256 (default, the headline); large: 1024 x 65536 interleaved; "
-                         "ragged: 100000 ADI systems of 32..8192 unknowns; serve: a served request stream")
+                         "ragged: 100000 ADI systems of 32..8192 unknowns; serve: a served request stream; "
+                         "kernel: one solver (--kernel) on one batch")
+    ap.add_argument("--kernel", default="cr", choices=KERNELS, help="kernel workload: the solver")
+    ap.add_argument("--system-size", type=int, default=N, help="kernel workload: unknowns per system")
+    ap.add_argument("--num-systems", type=int, default=M, help="kernel workload: systems")
+    ap.add_argument("--param", type=int, default=0, help="kernel workload: rest (crpcr) or gaussian (pcrGauss)")
+    ap.add_argument("--tunable", action="append", default=[], metavar="KEY=VALUE",
+                    help="kernel workload: tridi_set_tunable before the run (repeatable)")
     ap.add_argument("--ragged-count", type=int, default=100000, help="systems of the ragged workload")
     ap.add_argument("--sweeps", type=int, default=1, help="refinement sweeps of the ragged / serve workloads")
     ap.add_argument("--serve-requests", type=int, default=200, help="requests of the serve workload")
@@ -852,6 +928,8 @@ def main():
         return run_ragged(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "kernel":
+        return run_kernel(args)
     return run_gpu(args)
 
 
