@@ -435,6 +435,25 @@ def run_gpu(args):
         res = rel_residual64(a[:32], b[:32], c[:32], d[:32], hx[:32].numpy()).max()
         if not res < 2e-6:
             raise SystemExit(f"bench: drop-in cr result fails the residual check (residual {res:.2e})")
+    # the same from ordinary (pageable) host memory, as the reference's own
+    # callers allocate it (test_tridiagonal.cpp:34-39); x touched once first
+    px = np.ones_like(a)
+    pptrs = [v.ctypes.data for v in (a, b, c, d, px)]
+
+    def e2e_pageable_step():
+        _lib.check(lib.tridi_dropin_solve_f32(0, *pptrs, N, M, 0), "tridi_dropin_solve_f32")
+
+    e2e_pageable_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_pageable_step()
+    barrier(world)
+    e2e_pg_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world, dev)
+    if rank == 0:
+        res = rel_residual64(a[:32], b[:32], c[:32], d[:32], px[:32]).max()
+        if not res < 2e-6:
+            raise SystemExit(f"bench: pageable drop-in cr result fails the residual check (residual {res:.2e})")
 
     # ---- per-kernel tables (outside the timed region) ----
     peak, peak_kind = measured_peaks()
@@ -489,6 +508,9 @@ def run_gpu(args):
             "e2e": {"value": world * unknowns / e2e_s, "unit": "unknowns/s",
                     "h2d_bytes_per_step": 4 * unknowns * 4, "d2h_bytes_per_step": unknowns * 4,
                     "path": "tridi_dropin_solve_f32 (cr() drop-in), pinned host buffers"},
+            "e2e_pageable": {"value": world * unknowns / e2e_pg_s, "unit": "unknowns/s",
+                             "h2d_bytes_per_step": 4 * unknowns * 4, "d2h_bytes_per_step": unknowns * 4,
+                             "path": "the same drop-in from ordinary (pageable) numpy arrays"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": profile_traffic(), "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": BYTES_PER_UNKNOWN * unknowns},
