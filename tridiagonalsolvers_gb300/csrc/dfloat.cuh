@@ -102,4 +102,42 @@ __device__ __forceinline__ float df_residual(float a, float b, float c, float d,
   return __fadd_rn(st.x, t);
 }
 
+// ---- the same on two independent rows at once ----------------------------
+// Component-wise, operation for operation the scalar routines above, in the
+// paired FP32 instructions of sm_100+ (FADD2 / FMUL2 / FFMA2, round to nearest
+// like __fadd_rn / __fmul_rn / fmaf): bit-identical results, half the issue
+// slots.
+__device__ __forceinline__ float2 df2_neg(float2 v) { return make_float2(-v.x, -v.y); }
+__device__ __forceinline__ float2 two_sum2(float2 a, float2 b, float2& e) {
+  const float2 s = __fadd2_rn(a, b);
+  const float2 bb = __fadd2_rn(s, df2_neg(a));
+  e = __fadd2_rn(__fadd2_rn(a, df2_neg(__fadd2_rn(s, df2_neg(bb)))), __fadd2_rn(b, df2_neg(bb)));
+  return s;
+}
+// residual_parts for two rows.
+__device__ __forceinline__ void residual_parts2(float2 a, float2 b, float2 c, float2 d, float2 xm, float2 x0,
+                                                float2 xp, float2& s, float2& t) {
+  const float2 pb = __fmul2_rn(b, x0), pa = __fmul2_rn(a, xm), pc = __fmul2_rn(c, xp);
+  t = df2_neg(__fadd2_rn(__fadd2_rn(__ffma2_rn(b, x0, df2_neg(pb)), __ffma2_rn(a, xm, df2_neg(pa))),
+                         __ffma2_rn(c, xp, df2_neg(pc))));
+  float2 e;
+  s = two_sum2(d, df2_neg(pb), e);
+  t = __fadd2_rn(t, e);
+  s = two_sum2(s, df2_neg(pa), e);
+  t = __fadd2_rn(t, e);
+  s = two_sum2(s, df2_neg(pc), e);
+  t = __fadd2_rn(t, e);
+}
+// df_residual for two rows: x given as high words (xmh, x0h, xph) and low
+// words (xml, x0l, xpl), each pair holding the two rows.
+__device__ __forceinline__ float2 df_residual2(float2 a, float2 b, float2 c, float2 d, float2 xmh, float2 xml,
+                                               float2 x0h, float2 x0l, float2 xph, float2 xpl) {
+  float2 s, t;
+  residual_parts2(a, b, c, d, xmh, x0h, xph, s, t);
+  t = __ffma2_rn(df2_neg(b), x0l, t);
+  t = __ffma2_rn(df2_neg(a), xml, t);
+  t = __ffma2_rn(df2_neg(c), xpl, t);
+  return __fadd2_rn(s, t);
+}
+
 }  // namespace tridi

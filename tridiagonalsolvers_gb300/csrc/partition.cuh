@@ -109,6 +109,7 @@ struct ChunkSummary {
 // right-hand side functor is told the chunk's first row (start) and then
 // called for the chunk's rows in order.
 struct RhsStaged {
+  static constexpr bool kPairs = false;  // true: pair(i, row i, row i + 1) gives two rows' right-hand sides
   __device__ __forceinline__ void start(int) const {}
   template <class T>
   __device__ __forceinline__ T operator()(int, T, T, T, T d) const {
@@ -127,16 +128,37 @@ __device__ __forceinline__ void chunk_eliminate_smem(ChunkSummary<T>& cs, int k,
                                                      T* __restrict__ sc, T* __restrict__ sd,
                                                      const Rhs& rhs = Rhs()) {
   T cprev = T(0), aprev = T(0), dprev = T(0);
-#pragma unroll 4
-  for (int i = 0; i < k - 1; ++i) {
-    const T a0 = sa[i], b0 = sb[i], c0 = sc[i];
+  const auto step = [&](int i, T a0, T b0, T c0, T r) {
     const T a = (i == 0 && first) ? T(0) : a0;
     const T inv = tdiv(T(1), b0 - a * cprev);
     const T cn = c0 * inv;
     const T an = (i == 0 ? a : -a * aprev) * inv;
-    const T dn = (rhs(i, a0, b0, c0, sd[i]) - a * dprev) * inv;
+    const T dn = (r - a * dprev) * inv;
     sa[i] = an; sc[i] = cn; sd[i] = dn;
     cprev = cn; aprev = an; dprev = dn;
+  };
+  if constexpr (Rhs::kPairs) {
+    // the right-hand sides of rows i and i + 1 formed together (they do not
+    // depend on the elimination), the two rows then eliminated in order
+    int i = 0;
+#pragma unroll 2
+    for (; i + 1 < k - 1; i += 2) {
+      const T a0 = sa[i], b0 = sb[i], c0 = sc[i], d0 = sd[i];
+      const T a1 = sa[i + 1], b1 = sb[i + 1], c1 = sc[i + 1], d1 = sd[i + 1];
+      const auto r = rhs.pair(i, a0, b0, c0, d0, a1, b1, c1, d1);
+      step(i, a0, b0, c0, r.x);
+      step(i + 1, a1, b1, c1, r.y);
+    }
+    if (i < k - 1) {
+      const T a0 = sa[i], b0 = sb[i], c0 = sc[i];
+      step(i, a0, b0, c0, rhs(i, a0, b0, c0, sd[i]));
+    }
+  } else {
+#pragma unroll 4
+    for (int i = 0; i < k - 1; ++i) {
+      const T a0 = sa[i], b0 = sb[i], c0 = sc[i];
+      step(i, a0, b0, c0, rhs(i, a0, b0, c0, sd[i]));
+    }
   }
   T D = T(0), C = T(-1), A = T(0);
 #pragma unroll 4

@@ -299,6 +299,22 @@ __device__ __forceinline__ void warp_solve_rows(float* R, float* X, int m, int l
   chunk_back_smem<float>(q, sj, sl, ra, rc, rd, em);
 }
 
+// A system's right-hand side seen from the chunk starting at row r0 (chunk
+// row i is system row r0 + i).
+template <class Rhs>
+struct ChunkRhs {
+  const Rhs& rhs;
+  int r0;
+  static constexpr bool kPairs = Rhs::kPairs;
+  __device__ __forceinline__ float operator()(int i, float a, float b, float c, float d) const {
+    return rhs(r0 + i, a, b, c, d);
+  }
+  __device__ __forceinline__ float2 pair(int i, float a0, float b0, float c0, float d0, float a1, float b1, float c1,
+                                         float d1) const {
+    return rhs.pair(r0 + i, a0, b0, c0, d0, a1, b1, c1, d1);
+  }
+};
+
 template <class Emit, class Rhs = RhsStaged>
 __device__ __forceinline__ void group_solve(int n, int gt, int bar, int gtid, float* sa, const float* sb, float* sc,
                                             float* sd, float* R, float* X, float* F0, Emit& emit,
@@ -310,9 +326,8 @@ __device__ __forceinline__ void group_solve(int n, int gt, int bar, int gtid, fl
   kr = kr < 0 ? 0 : (kr > kk ? kk : kr);
   ChunkSummary<float> cs;
   rhs.start(r0);
-  const auto chunk_rhs = [&](int i, float a, float b, float c, float d) { return rhs(r0 + i, a, b, c, d); };
   chunk_eliminate_smem<float>(cs, kr, gtid == 0, r0 + kr == n && kr > 0, sa + r0, sb + r0, sc + r0, sd + r0,
-                              chunk_rhs);
+                              ChunkRhs<Rhs>{rhs, r0});
   float nD = __shfl_down_sync(kFull, cs.fD, 1);
   float nC = __shfl_down_sync(kFull, cs.fC, 1);
   float nA = __shfl_down_sync(kFull, cs.fA, 1);
@@ -400,6 +415,7 @@ template <int MODE>
 struct RhsResidual;
 template <>
 struct RhsResidual<kRefineDF> {
+  static constexpr bool kPairs = false;
   XStore<kRefineDF> xs;
   int n;
   mutable float2 xm, x0;
@@ -420,6 +436,7 @@ struct RhsResidual<kRefineDF> {
 };
 template <>
 struct RhsResidual<kRefineFP64> {
+  static constexpr bool kPairs = false;
   XStore<kRefineFP64> xs;
   int n;
   mutable double xm, x0;
@@ -514,6 +531,7 @@ __device__ __forceinline__ void group_refine(const RagParams& p, const RagSys& s
 // words), rows of a chunk in order, x0_{i-1} and x0_i carried.
 template <int M>
 struct RhsResidual1 {
+  static constexpr bool kPairs = M == kRefineDF;
   const float* x0w;
   int n;
   mutable float xm, x0;
@@ -539,7 +557,114 @@ struct RhsResidual1 {
     x0 = xp;
     return r;
   }
+  // Rows i and i + 1, both interior rows of a chunk (so 0 < i + 1 and
+  // i + 2 < n: only row i's a can lie outside the system), in paired
+  // instructions: residual_parts2 is residual_parts component by component.
+  __device__ __forceinline__ float2 pair(int i, float a0, float b0, float c0, float d0, float a1, float b1, float c1,
+                                         float d1) const {
+    const float x1 = x0w[i + 1], x2 = x0w[i + 2];
+    float2 s, t;
+    residual_parts2(make_float2(i > 0 ? a0 : 0.f, a1), make_float2(b0, b1), make_float2(c0, c1),
+                    make_float2(d0, d1), make_float2(xm, x0), make_float2(x0, x1), make_float2(x1, x2), s, t);
+    xm = x1;
+    x0 = x2;
+    return __fadd2_rn(s, t);
+  }
 };
+
+// The last pass of the one-correction modes: x = x0 + e (x0 in the ring's b
+// words xw, e in its d words ew), its residual d - T x, the group's
+// ||d - T x|| / ||d|| folded into the CTA's maximum, and x written as FP64.
+// Rows i = gtid + q gt; the original a, b, c, d come from global memory (L2,
+// coalesced across the group), each thread keeping the loads of its next
+// kAhead rows in flight.  The double-float form takes its rows two at a time
+// (i and i + gt) in paired FP32 instructions, the same operations as the
+// scalar form component by component.
+template <int M>
+__device__ __forceinline__ void refine1_final(const RagParams& p, const RagSys& sy, int gt, int bar, int gtid,
+                                              const float* xw, const float* ew, double* red) {
+  const int n = sy.n;
+  const float* ga = p.a + sy.off;
+  const float* gb = p.b + sy.off;
+  const float* gc = p.c + sy.off;
+  const float* gd = p.d + sy.off;
+  double* xo = p.x64 + sy.off;
+  constexpr int kAhead = 4;  // two pairs
+  float na[kAhead], nb[kAhead], nc[kAhead], nd[kAhead];
+#pragma unroll
+  for (int q = 0; q < kAhead; ++q) {
+    const int j = gtid + q * gt;
+    const bool in = j < n;
+    na[q] = in ? ga[j] : 0.f;
+    nb[q] = in ? gb[j] : 0.f;
+    nc[q] = in ? gc[j] : 0.f;
+    nd[q] = in ? gd[j] : 0.f;
+  }
+  float2 rr = make_float2(0.f, 0.f), dd = make_float2(0.f, 0.f);
+  const auto out = [&](int i, float h0, float e0) {
+    float l;
+    const float h = two_sum(h0, e0, l);
+    xo[i] = df_to_double(h, l);
+  };
+  for (int i0 = gtid; i0 < n; i0 += kAhead * gt) {
+#pragma unroll
+    for (int q = 0; q < kAhead; q += 2) {
+      const int i = i0 + q * gt, j = i + gt;  // j > 0
+      if (i >= n) break;
+      const bool jin = j < n;
+      float2 a = make_float2(na[q], na[q + 1]), b = make_float2(nb[q], nb[q + 1]);
+      float2 c = make_float2(nc[q], nc[q + 1]), d = make_float2(nd[q], nd[q + 1]);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int f = i + (u + kAhead) * gt;
+        if (f < n) {
+          na[q + u] = ga[f];
+          nb[q + u] = gb[f];
+          nc[q + u] = gc[f];
+          nd[q + u] = gd[f];
+        }
+      }
+      if (i == 0) a.x = 0.f;
+      if (i == n - 1) c.x = 0.f;
+      if (j >= n - 1) c.y = 0.f;
+      // x words of rows i - 1, i, i + 1 and j - 1, j, j + 1 (zero outside the system)
+      const float2 xmh = make_float2(i > 0 ? xw[i - 1] : 0.f, jin ? xw[j - 1] : 0.f);
+      const float2 xml = make_float2(i > 0 ? ew[i - 1] : 0.f, jin ? ew[j - 1] : 0.f);
+      const float2 x0h = make_float2(xw[i], jin ? xw[j] : 0.f);
+      const float2 x0l = make_float2(ew[i], jin ? ew[j] : 0.f);
+      const float2 xph = make_float2(i + 1 < n ? xw[i + 1] : 0.f, j + 1 < n ? xw[j + 1] : 0.f);
+      const float2 xpl = make_float2(i + 1 < n ? ew[i + 1] : 0.f, j + 1 < n ? ew[j + 1] : 0.f);
+      float2 r;
+      if constexpr (M == kRefineFP64) {
+        const auto x64 = [](float h0, float e0) {
+          float l;
+          const float h = two_sum(h0, e0, l);
+          return df_to_double(h, l);
+        };
+        const auto res = [&](float a1, float b1, float c1, float d1, double m1, double z1, double p1) {
+          double v = fma(-f2d_exact(b1), z1, f2d_exact(d1));
+          v = fma(-f2d_exact(a1), m1, v);
+          v = fma(-f2d_exact(c1), p1, v);
+          return (float)v;
+        };
+        r.x = res(a.x, b.x, c.x, d.x, x64(xmh.x, xml.x), x64(x0h.x, x0l.x), x64(xph.x, xpl.x));
+        r.y = jin ? res(a.y, b.y, c.y, d.y, x64(xmh.y, xml.y), x64(x0h.y, x0l.y), x64(xph.y, xpl.y)) : 0.f;
+      } else {
+        r = df_residual2(a, b, c, d, xmh, xml, x0h, x0l, xph, xpl);
+      }
+      if (!jin) {  // no row j: its prefetch registers may hold an earlier row
+        r.y = 0.f;
+        d.y = 0.f;
+      }
+      rr = __ffma2_rn(r, r, rr);
+      dd = __ffma2_rn(d, d, dd);
+      out(i, x0h.x, x0l.x);
+      if (jin) out(j, x0h.y, x0l.y);
+    }
+  }
+  group_rel_max(rr.x + rr.y, dd.x + dd.y, gt, bar, gtid, reinterpret_cast<float*>(red),
+                reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps));
+}
 
 // One-correction refinement (sweeps == 1) of one staged system by its solve
 // group, in the ring's four arrays: the FP32 solve leaves x0 in the b words;
@@ -557,67 +682,14 @@ __device__ __forceinline__ void group_refine1(const RagParams& p, const RagSys& 
   const int pad = (int)(sy.off - lo);
   const uint32_t bytes = (uint32_t)(4 * (hi - lo));
   const float* gb = p.b + sy.off;
-  const float* gd = p.d + sy.off;
   EmitStore to_b{sb};
   group_solve(n, gt, bar, gtid, sa, sb, sc, sd, R, X, F0, to_b);
   restage(Restage{mb, pbit, sa - pad, sc - pad, sd - pad, p.a + lo, p.c + lo, p.d + lo, bytes, true}, par, gt, bar,
           gtid, p.status);
   EmitOverD to_d;
   group_solve(n, gt, bar, gtid, sa, gb, sc, sd, R, X, F0, to_d, RhsResidual1<M>{sb, n});
-  // The final pass reads b and d from global memory (L2): each thread keeps
-  // the loads of its next kAhead rows in flight, the first ones issued
-  // before the re-staging wait.
-  constexpr int kAhead = 4;
-  float nb[kAhead], nd[kAhead];
-#pragma unroll
-  for (int q = 0; q < kAhead; ++q) {
-    const int j = gtid + q * gt;
-    nb[q] = j < n ? gb[j] : 0.f;
-    nd[q] = j < n ? gd[j] : 0.f;
-  }
-  restage(Restage{mb, pbit, sa - pad, sc - pad, sd - pad, p.a + lo, p.c + lo, p.d + lo, bytes, false}, par, gt, bar,
-          gtid, p.status);
-  float rr = 0.f, dd = 0.f;
-  double* xo = p.x64 + sy.off;
-  for (int i0 = gtid; i0 < n; i0 += kAhead * gt) {
-#pragma unroll
-    for (int q = 0; q < kAhead; ++q) {
-      const int i = i0 + q * gt;
-      if (i >= n) break;
-      const float b = nb[q], d = nd[q];
-      const int j = i + kAhead * gt;
-      if (j < n) {
-        nb[q] = gb[j];
-        nd[q] = gd[j];
-      }
-      const float a = i > 0 ? sa[i] : 0.f, c = i < n - 1 ? sc[i] : 0.f;
-      // x = x0 + e: the pair's low word is within a few ulps of the high one
-      const float2 xm = i > 0 ? make_float2(sb[i - 1], sd[i - 1]) : make_float2(0.f, 0.f);
-      const float2 x0 = make_float2(sb[i], sd[i]);
-      const float2 xp = i < n - 1 ? make_float2(sb[i + 1], sd[i + 1]) : make_float2(0.f, 0.f);
-      float r;
-      if constexpr (M == kRefineFP64) {
-        const auto x64 = [](float2 v) {
-          float l;
-          const float h = two_sum(v.x, v.y, l);
-          return df_to_double(h, l);
-        };
-        double v = fma(-f2d_exact(b), x64(x0), f2d_exact(d));
-        v = fma(-f2d_exact(a), x64(xm), v);
-        v = fma(-f2d_exact(c), x64(xp), v);
-        r = (float)v;
-      } else {
-        r = df_residual(a, b, c, d, xm, x0, xp);
-      }
-      rr = fmaf(r, r, rr);
-      dd = fmaf(d, d, dd);
-      float l;
-      const float h = two_sum(x0.x, x0.y, l);
-      xo[i] = df_to_double(h, l);
-    }
-  }
-  group_rel_max(rr, dd, gt, bar, gtid, reinterpret_cast<float*>(red),
-                reinterpret_cast<unsigned long long*>(red + 2 * kRagWarps));
+  if (gt == 32) __syncwarp();  // the e words are complete (group_solve ends on the barrier otherwise)
+  refine1_final<M>(p, sy, gt, bar, gtid, sb, sd, red);
 }
 
 // A BIG system (rows read straight from global memory, right-hand side rhs):
@@ -732,7 +804,11 @@ __device__ __forceinline__ void big_refine(const RagParams& p, const RagSys& sy,
 }
 
 // ---------------------------------------------------------------------------
-template <int MODE>
+// BIG: the kernel carries the BIG-item path.  Its register demand (kBigChunks
+// chunk states per thread) would set the allocation of the whole kernel and
+// push values of the other items' solve loops into local memory, so plans
+// without BIG items run the kernel compiled without it.
+template <int MODE, bool BIG>
 __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p) {
   static_assert((kRagThreads + 32) % 128 == 0, "16 warps: 4 per SM sub-partition");
   constexpr int RR = ring_rows(MODE);
@@ -905,6 +981,8 @@ __global__ void __launch_bounds__(kRagThreads + 32, 1) ragged_kernel(RagParams p
           group_refine<MODE>(p, sy, kRagThreads, 1, tid, A + base, B + base, C + base, D + base, XH + base, XL + base,
                              Rsh, Xsh, F0, red, &rbar[kRagWarps + kTeams], kRagWarps + kTeams, rpar);
         }
+      } else if constexpr (!BIG) {  // the host launches this form only for plans without BIG items
+        record_error(p.status, TRIDI_DEVERR_BAD_PLAN);
       } else {  // kBig
         const int rb = ds.rbase;
         float* Ra = A + rb;
@@ -983,6 +1061,11 @@ struct RaggedPlan {
   std::vector<RagSys> sys;
   long total_rows = 0;
   int num_systems = 0;
+  bool has_big = false;     // an item of kind kBig
+  int max_single_rows = 0;  // ring rows of the largest SINGLE item
+  // BIG items in a launch whose ring holds `ring_rows` rows per array (a
+  // SINGLE item beyond it is solved as BIG)
+  bool needs_big(int ring_rows) const { return has_big || max_single_rows > ring_rows; }
   size_t device_bytes() const {
     return 64 + items.size() * sizeof(RagItem) + sys.size() * sizeof(RagSys);
   }
@@ -1081,6 +1164,10 @@ tridi_status plan_create(const long* offsets, int num_systems, bool refine, void
     }
     team_items.push_back(it);
   }
+  for (const RagItem& it : cta_items) {
+    if (it.kind == kBig) plan->has_big = true;
+    if (it.kind == kSingle) plan->max_single_rows = std::max(plan->max_single_rows, it.rows);
+  }
   plan->items = std::move(cta_items);
   plan->items.insert(plan->items.end(), team_items.begin(), team_items.end());
   *plan_out = plan;
@@ -1163,9 +1250,9 @@ tridi_status ragged_launch(const RaggedPlan* plan, void* dev_plan, RagParams& p,
   if (!dev) return TRIDI_ERROR_CUDA;
   const size_t smem = rag_smem_bytes(MODE);
   if (smem > (size_t)dev->max_smem_optin) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  const auto kernel = plan->needs_big(ring_rows(MODE)) ? ragged_kernel<MODE, true> : ragged_kernel<MODE, false>;
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(ragged_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-      cudaSuccess)
+  if ((e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
     return cuda_status(e);
   char* dp = static_cast<char*>(dev_plan);
   p.items = reinterpret_cast<const RagItem*>(dp + 64);
@@ -1174,7 +1261,7 @@ tridi_status ragged_launch(const RaggedPlan* plan, void* dev_plan, RagParams& p,
   p.status = dev->status;
   int grid = dev->sm_count;
   if (grid > p.nitems) grid = p.nitems;
-  ragged_kernel<MODE><<<grid, kRagThreads + 32, smem, st>>>(p);
+  kernel<<<grid, kRagThreads + 32, smem, st>>>(p);
   return cuda_status(cudaGetLastError());
 }
 
