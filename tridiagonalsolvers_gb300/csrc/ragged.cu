@@ -36,9 +36,9 @@
 // Arithmetic: the partition solver of partition.cuh, per warp (MULTI), per
 // team of 160 threads (GROUP) or per CTA (SINGLE), with the chunk
 // elimination done in place in the ring (no register arrays, so no bound on
-// rows per thread) and the separators solved by PCR in shuffles (warp), by
-// one warp of the team (group: a 5-row chunk per lane, then PCR in
-// shuffles), or by PCR in shared memory (CTA).
+// rows per thread) and the separators solved by PCR in shuffles (warp), or
+// by one warp of the group from shared memory (team and CTA: a 5- or 15-row
+// chunk per lane, then PCR in shuffles).
 //
 // Refined modes (tridi_ragged_refine_f32): every system is refined where it
 // sits, without leaving the SM: FP32 solve -> x; then `sweeps` times
@@ -268,8 +268,9 @@ __device__ __forceinline__ void group_rel_max(float rr, float dd, int gt, int ba
 // One system of n rows (ring arrays sa..sd, overwritten) solved by a group of
 // gt threads (thread gtid of the group; gt == 32: one warp, else the named
 // barrier `bar` over the group): chunk elimination in place, the gt
-// separators solved by PCR (warp shuffles, or shared memory R: 4*gt floats,
-// X: gt, F0: 3*(gt/32)), back substitution; emit(i, x_i) for every row.
+// separators solved by PCR in warp shuffles (gt == 32) or by one warp of the
+// group (warp_solve_rows over shared memory R: 4*gt floats, X: gt, F0:
+// 3*(gt/32)), back substitution; emit(i, x_i) for every row.
 // Emit tag: x_i written over the ring's d_i.
 struct EmitOverD {};
 
@@ -345,30 +346,15 @@ __device__ __forceinline__ void group_solve(int n, int gt, int bar, int gtid, fl
       nD = F0[(gw + 1) * 3 + 0]; nC = F0[(gw + 1) * 3 + 1]; nA = F0[(gw + 1) * 3 + 2];
     }
     Row<float> sr = separator_row_s<float>(cs, nD, nC, nA);
-    if (gt <= kTeamThreads) {  // one warp solves the separators, the others wait at the barrier
-      R[gtid] = sr.a; R[gt + gtid] = sr.b; R[2 * gt + gtid] = sr.c; R[3 * gt + gtid] = sr.d;
-      group_sync(bar, gt);
-      if (gw == 0) warp_solve_rows(R, X, gt, lane);
-      group_sync(bar, gt);
-      sj = X[gtid];
-    } else {  // the whole CTA: PCR, log2(gt) steps (shorter than one warp's chain over 15 rows per lane)
-      const Row<float> id{0.f, 1.f, 0.f, 0.f};
-      for (int dl = 1; dl < gt; dl *= 2) {
-        R[gtid] = sr.a; R[gt + gtid] = sr.b; R[2 * gt + gtid] = sr.c; R[3 * gt + gtid] = sr.d;
-        group_sync(bar, gt);
-        const Row<float> L = gtid >= dl ? Row<float>{R[gtid - dl], R[gt + gtid - dl], R[2 * gt + gtid - dl],
-                                                     R[3 * gt + gtid - dl]}
-                                        : id;
-        const Row<float> Rr = gtid + dl < gt ? Row<float>{R[gtid + dl], R[gt + gtid + dl], R[2 * gt + gtid + dl],
-                                                          R[3 * gt + gtid + dl]}
-                                             : id;
-        sr = reduce_row(sr, L, Rr);
-        group_sync(bar, gt);
-      }
-      sj = tdiv(sr.d, sr.b);
-      X[gtid] = sj;
-      group_sync(bar, gt);
-    }
+    // one warp solves the separators (gt / 32 rows per lane: 5 for a team,
+    // 15 for the CTA), the others wait at the barrier: measured faster than
+    // a PCR over the CTA's 480 rows in shared memory (9 steps, each two
+    // barriers of all 15 warps)
+    R[gtid] = sr.a; R[gt + gtid] = sr.b; R[2 * gt + gtid] = sr.c; R[3 * gt + gtid] = sr.d;
+    group_sync(bar, gt);
+    if (gw == 0) warp_solve_rows(R, X, gt, lane);
+    group_sync(bar, gt);
+    sj = X[gtid];
     sl = gtid > 0 ? X[gtid - 1] : 0.f;
   }
   if constexpr (std::is_same_v<Emit, EmitOverD>) {
