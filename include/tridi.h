@@ -73,9 +73,9 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
 #define TRIDI_RESIDUAL_DF 1     /*   double-float (pairs of FP32, 48-bit significand; the default) */
 #define TRIDI_RESIDUAL_FP64 2   /*   native FP64 */
 #define TRIDI_TUNE_SERVER_COPY 5  /* host<->device transfer of servers created afterwards: */
-#define TRIDI_SERVER_COPY_MEMCPY 1 /*   1 = cudaMemcpyAsync on the callers' arrays; */
+#define TRIDI_SERVER_COPY_MEMCPY 1 /*   0 or 1 = cudaMemcpyAsync on the callers' arrays; */
 #define TRIDI_SERVER_COPY_DIRECT 2 /*   2 = kernels read / write the callers' arrays (pageable memory access); */
-#define TRIDI_SERVER_COPY_STAGED 3 /*   0 or 3 = pinned double-buffered staging filled by host threads */
+#define TRIDI_SERVER_COPY_STAGED 3 /*   3 = pinned double-buffered staging filled by host threads */
 #define TRIDI_TUNE_LARGE_TMA 6    /* interleaved FP32 large systems: 0/1 = TMA-tiled passes where they apply, 2 = off */
 #define TRIDI_TUNE_WARP_STREAMS 7 /* CR/PCR/CR-PCR with a system per warp or less: 0/1 = every warp streams its own
                                      systems (no producer warp), 2 = CTA ring filled by a producer warp */
