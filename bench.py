@@ -323,7 +323,7 @@ def kernel_table(lib, m: int, n: int, seed: int, dev, peak: float, with_referenc
     r32 = min(32, n // 2)
     ours[f"crpcrNBC_rest{r32}"] = lambda: lib.tridi_crpcr_nbc_f32(*wp, n, m, r32, sp)
     rows.append((f"crpcrNBC_rest{r32}", "crpcrNBC", r32))
-    for g in sorted({8, min(n // 2, 512)}):
+    for g in sorted({8, 64, min(n // 2, 512)}):  # 64: the reference driver's own call (test_tridiagonal.cpp:81)
         ours[f"pcrGauss_g{g}"] = (lambda gg: lambda: lib.tridi_pcr_thomas_f32(*wp, n, m, gg, sp))(g)
         rows.append((f"pcrGauss_g{g}", "pcrGauss", g))
     rk = None

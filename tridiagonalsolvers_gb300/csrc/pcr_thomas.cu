@@ -218,6 +218,10 @@ tridi_status pcr_thomas_device(const T* a, const T* b, const T* c, const T* d, T
   // (j, j + n/2) that close PCR (g = n: one more step decouples every row,
   // the same solution), so the register PCR kernels solve it.
   if (pcr_shape && g >= n / 2) return hybrid_solve_device<T>(a, b, c, d, x, n, m, 1, stream);
+  // FP32, 64 .. 1024 unknowns: the register kernel on the two-phase PCR layout
+  if constexpr (sizeof(T) == 4) {
+    if (pcr_thomas2_applies(a, b, c, d, n, m, g)) return pcr_thomas2_solve(a, b, c, d, x, n, m, g, as_stream(stream));
+  }
   const DeviceInfo* dev = current_device();
   if (!dev) return TRIDI_ERROR_CUDA;
   PTParams p{};

@@ -39,6 +39,11 @@ int tuned(int table, int log2key);
 // Ragged plans: the largest padded row count a warp or team item may hold
 // (larger systems always take a whole CTA, whatever the threads table says).
 long ragged_team_max_rows();
+// PCR-then-Thomas in registers (pcr_thomas2.cu): whether it takes an FP32
+// call, and the launch.
+bool pcr_thomas2_applies(const void* a, const void* b, const void* c, const void* d, int n, long m, int g);
+tridi_status pcr_thomas2_solve(const float* a, const float* b, const float* c, const float* d, float* x, int n,
+                               int m, int g, cudaStream_t stream);
 
 inline int ilog2(long v) {
   int k = 0;
