@@ -12,7 +12,8 @@ Lines printed (rank 0, one JSON line):
   * value: device-resident throughput (CUDA events around K back-to-back
     steps on the launching stream, max over ranks);
   * e2e: the same through the reference-facing host-pointer launcher
-    (tridi_dropin_solve_f32 = cr()), pinned host buffers, host<->device copies
+    (tridi_dropin_solve_f32 = cr()), pinned host buffers (which the solver
+    reads and writes in place over the host link), every byte's transfer
     inside the timed region;
   * roofline, cpu_baseline, clocks, per-kernel table (cr, crNBC, pcr, crpcr
     over its switch levels) for the same batch.
@@ -513,7 +514,8 @@ def run_gpu(args):
                        "seed": workloads.SEEDS["c2"], "parallelism": f"replicas x{world} (independent batches)"},
             "e2e": {"value": world * unknowns / e2e_s, "unit": "unknowns/s",
                     "h2d_bytes_per_step": 4 * unknowns * 4, "d2h_bytes_per_step": unknowns * 4,
-                    "path": "tridi_dropin_solve_f32 (cr() drop-in), pinned host buffers"},
+                    "path": "tridi_dropin_solve_f32 (cr() drop-in), pinned host buffers, which the solver "
+                            "reads and writes in place over the host link (no staging copies)"},
             "e2e_pageable": {"value": world * unknowns / e2e_pg_s, "unit": "unknowns/s",
                              "h2d_bytes_per_step": 4 * unknowns * 4, "d2h_bytes_per_step": unknowns * 4,
                              "path": "the same drop-in from ordinary (pageable) numpy arrays"},

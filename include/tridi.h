@@ -88,6 +88,10 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
                                      once between the register phases) with paired FP32 instructions,
                                      3 = the same on single rows, 2 = the hybrid warp kernel (the same
                                      algorithm throughout; results differ in rounding only) */
+#define TRIDI_TUNE_DROPIN_MAPPED 11 /* host-pointer launchers (cr, pcr, crpcr, crNBC, crNBC32, crpcrNBC):
+                                     0/1 = arrays that are pinned and mapped into the device's address
+                                     space are read and written in place by the solver (no staging
+                                     copies), 2 = always staged through device memory */
 tridi_status tridi_set_tunable(int key, int value);
 int tridi_get_tunable(int key);
 

@@ -28,7 +28,11 @@
  * What changed underneath: no cudaMalloc/cudaFree per call (a persistent
  * device workspace that grows on demand, guarded by a mutex), and the batch is
  * split into chunks whose host->device copy, solve and device->host copy
- * overlap on three streams.  The solver kernels themselves are in tridi.h.
+ * overlap on three streams.  Arrays that are pinned and mapped into the
+ * device's address space (cudaHostAlloc, cudaHostRegister with mapping) are
+ * instead read and written in place by the solver over the host link, without
+ * staging copies (all launchers but pcrGaussWrapper; TRIDI_TUNE_DROPIN_MAPPED
+ * in tridi.h turns it off).  The solver kernels themselves are in tridi.h.
  *
  * pcrGaussWrapper takes any systemSize >= 1, as the reference's does (its
  * large path, pcrGauss_app.cu:196-228, takes every size above MINSYSTEM =

@@ -186,3 +186,46 @@ def test_dropin_rejects_bad_sizes(cuda):
     a = np.zeros((2, 300), np.float32)
     with pytest.raises(tg.TridiError):
         dropin.cr(a, a.copy(), a.copy(), a.copy(), a.copy(), 300, 2)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("n", [256, 1024])
+def test_dropin_pinned_arrays_solved_in_place(cuda, prec, n):
+    """Pinned, mapped host arrays (torch's pin_memory): the launchers solve them
+    in place over the host link (TRIDI_TUNE_DROPIN_MAPPED, key 11); the same
+    calls staged through device memory (key 11 = 2) agree -- bit for bit where
+    both paths run the same CR arithmetic -- and a..d are left unchanged."""
+    import torch
+
+    from tridiagonalsolvers_gb300._lib import lib
+
+    dt = NP[prec]
+    m = 300
+    a, b, c, d = workloads.dominant(m, n, seed=77 + n, dtype=dt)
+
+    def pinned(v):
+        return torch.from_numpy(np.ascontiguousarray(v).reshape(-1).copy()).pin_memory().numpy()
+
+    pa, pb, pc, pd = (pinned(v) for v in (a, b, c, d))
+    launchers = [("cr", dropin.cr, ()), ("pcr", dropin.pcr, ()), ("crpcr", dropin.crpcr, (32,)),
+                 ("crNBC", dropin.crNBC, ()), ("crNBC32", dropin.crNBC32, ()),
+                 ("crpcrNBC", dropin.crpcrNBC, (32,))]
+    L = lib()
+    for name, fn, extra in launchers:
+        x_in = pinned(np.zeros(m * n, dt))
+        fn(pa, pb, pc, pd, x_in, n, m, *extra)
+        x_st = pinned(np.zeros(m * n, dt))
+        assert L.tridi_set_tunable(11, 2) == 0
+        try:
+            fn(pa, pb, pc, pd, x_st, n, m, *extra)
+        finally:
+            L.tridi_set_tunable(11, 0)
+        check_against_oracle(a, b, c, d, x_in.reshape(m, n), dtype=dt)
+        check_against_oracle(a, b, c, d, x_st.reshape(m, n), dtype=dt)
+        if name == "pcr":  # staged: the two-phase PCR kernel; in place: the hybrid kernel's PCR
+            check_ulps(x_in.reshape(m, n), x_st.reshape(m, n), ulps=64)
+        else:
+            assert np.array_equal(x_in, x_st), name
+    for p, v in zip((pa, pb, pc, pd), (a, b, c, d)):
+        assert np.array_equal(p, np.ascontiguousarray(v).reshape(-1))
+    assert tg.device_status() == 0

@@ -69,6 +69,18 @@ cudaError_t ensure_workspace(Workspace& w, size_t bytes) {
 
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
+// The device's address of host memory that is pinned and mapped into its
+// address space (cudaHostAlloc, cudaHostRegister with mapping), else null.
+template <class P>
+P* mapped_view(P* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();  // unregistered memory on older drivers: not an error of the call
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? static_cast<P*>(at.devicePointer) : nullptr;
+}
+
 // Extra device scratch the algorithm needs for m systems of size n.
 template <class T>
 size_t algo_scratch(int algo, int n, int m, int param);
@@ -87,6 +99,27 @@ tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d
   if (dev < 0 || dev >= kMaxDev) return TRIDI_ERROR_INVALID_VALUE;
   std::lock_guard<std::mutex> lock(g_mu);
   Workspace& w = g_ws[dev];
+
+  // Arrays that are pinned and mapped: the solver reads a..d and writes x in
+  // place over the host link.  The same bytes cross it as with staging
+  // copies, but no chunk pipeline fills and drains, and no copy waits for
+  // the copy engine behind another.  The kernels then read with plain loads
+  // (g_host_mapped_io); pcrGauss, whose larger sizes take the partition and
+  // large-system solvers, always stages.
+  if (!whole_batch_scratch && algo != TRIDI_DROPIN_PCR_THOMAS && tunable(TRIDI_TUNE_DROPIN_MAPPED) != 2) {
+    const T *va = mapped_view(a), *vb = mapped_view(b), *vc = mapped_view(c), *vd = mapped_view(d);
+    T* vx = mapped_view(x);
+    if (va && vb && vc && vd && vx) {
+      e = ensure_workspace(w, 0);
+      if (e != cudaSuccess) return cuda_status(e);
+      g_host_mapped_io = true;
+      tridi_status st = dropin_device_solve<T>(algo, va, vb, vc, vd, vx, n, m, param, nullptr, 0, w.stream[1]);
+      g_host_mapped_io = false;
+      const cudaError_t es = cudaStreamSynchronize(w.stream[1]);
+      if (st == TRIDI_SUCCESS && es != cudaSuccess) st = cuda_status(es);
+      return st;
+    }
+  }
 
   // Chunks of about 32 MiB of input (8 MiB per coefficient array, or
   // TRIDI_TUNE_DROPIN_CHUNK KiB), whole systems, at most 64 chunks.

@@ -96,7 +96,7 @@ cudaError_t launch_one(const HybridParams& p0, const DeviceInfo& dev, cudaStream
   auto kern = hybrid_kernel<T, K, WARP, LSTRIDE, MAXT, MINB>;
   HybridParams p = p0;
   const bool tma_ok = aligned16(p.a) && aligned16(p.b) && aligned16(p.c) && aligned16(p.d) && aligned16(p.x) &&
-                      ((size_t)p.n * sizeof(T)) % 16 == 0;
+                      ((size_t)p.n * sizeof(T)) % 16 == 0 && !g_host_mapped_io;
   // (FP32 shapes that keep their registers at 20 warps per SM; the FP64
   // shapes and PCR on 16 rows per thread would spill)
   if constexpr (WARP && sizeof(T) == 4 && !(K == 16 && LSTRIDE == 1)) {
@@ -159,7 +159,7 @@ bool pcr_twophase_applies(const HybridParams& p) {
   if constexpr (sizeof(T) != 4) return false;
   return p.stride == 1 && (p.n == 64 || p.n == 128 || p.n == 256 || p.n == 512 || p.n == 1024) && aligned16(p.a) &&
          aligned16(p.b) && aligned16(p.c) && aligned16(p.d) && (long)p.m * p.n / 32 < (1L << 31) &&
-         tunable(TRIDI_TUNE_PCR_KERNEL) != 2;
+         tunable(TRIDI_TUNE_PCR_KERNEL) != 2 && !g_host_mapped_io;
 }
 
 template <class T>

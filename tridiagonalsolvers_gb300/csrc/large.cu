@@ -223,7 +223,8 @@ tridi_status large_solve_device(const T* a, const T* b, const T* c, const T* d, 
   const unsigned blocks = (unsigned)((PM + 255) / 256);
   // interleaved FP32 with m a multiple of 32: the TMA-tiled passes (large_tma.cu)
   bool tma = false;
-  if constexpr (sizeof(T) == 4) tma = layout == 1 && tunable(TRIDI_TUNE_LARGE_TMA) != 2 && large_tma_ok(a, b, c, d, n, m);
+  if constexpr (sizeof(T) == 4)
+    tma = layout == 1 && tunable(TRIDI_TUNE_LARGE_TMA) != 2 && !g_host_mapped_io && large_tma_ok(a, b, c, d, n, m);
   if (tma) {
     // the separator rows assembled in the pass (the interface area holds the
     // tile-boundary arrays only)

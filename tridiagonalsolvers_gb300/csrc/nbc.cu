@@ -39,7 +39,7 @@ tridi_status solve_nbc(const T* a, const T* b, const T* c, const T* d, T* x, int
   p.n = n; p.m = m; p.rest = rest;
   p.status = dev->status;
   const bool tma_ok = aligned16(a) && aligned16(b) && aligned16(c) && aligned16(d) &&
-                      ((size_t)n * sizeof(T)) % 16 == 0;
+                      ((size_t)n * sizeof(T)) % 16 == 0 && !g_host_mapped_io;
   p.vec = aligned16(x) ? 1 : 0;
   const size_t limit = (size_t)dev->max_smem_optin;
   const size_t target = 110 * 1024;  // two CTAs per SM when it fits

@@ -162,7 +162,7 @@ cudaError_t launch_part(PartParams p, const DeviceInfo& dev, cudaStream_t stream
   constexpr int MINB = CTA ? 1 : 4;
   auto kern = partition_kernel<T, K, CTA, MAXT, MINB>;
   const bool tma_ok = aligned16(p.a) && aligned16(p.b) && aligned16(p.c) && aligned16(p.d) &&
-                      ((size_t)p.n * sizeof(T)) % 16 == 0;
+                      ((size_t)p.n * sizeof(T)) % 16 == 0 && !g_host_mapped_io;
   const size_t stage = (size_t)4 * p.G * p.n * sizeof(T);
   const size_t fixed = part_smem_bytes<T>(0, p.G, p.n, p.ct, CTA);
   const int S = tma_ok ? pick_stages(fixed, stage, 2, dev) : 0;

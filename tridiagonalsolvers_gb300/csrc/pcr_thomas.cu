@@ -244,7 +244,7 @@ tridi_status pcr_thomas_device(const T* a, const T* b, const T* c, const T* d, T
   p.ct = p.G * tps;
   p.ntiles = (int)(((long)m + p.G - 1) / p.G);
   const bool tma_ok = aligned16(a) && aligned16(b) && aligned16(c) && aligned16(d) &&
-                      ((size_t)n * sizeof(T)) % 16 == 0;
+                      ((size_t)n * sizeof(T)) % 16 == 0 && !g_host_mapped_io;
   int S = tma_ok ? 2 : 0;
   while (S > 0 && pt_smem<T>(S, p.G, n) > (size_t)dev->max_smem_optin) --S;
   if (pt_smem<T>(S, p.G, n) > (size_t)dev->max_smem_optin) return TRIDI_ERROR_UNSUPPORTED_SIZE;

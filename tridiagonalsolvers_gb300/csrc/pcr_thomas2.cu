@@ -249,7 +249,7 @@ cudaError_t launch_for_n(const HybridParams& p, int g, const DeviceInfo& dev, cu
 bool pcr_thomas2_applies(const void* a, const void* b, const void* c, const void* d, int n, long m, int g) {
   return (n == 64 || n == 128 || n == 256 || n == 512 || n == 1024) && g >= 1 && g < n / 2 && aligned16(a) &&
          aligned16(b) && aligned16(c) && aligned16(d) && m * n / 32 < (1L << 31) &&
-         tunable(TRIDI_TUNE_PCR_KERNEL) != 2;
+         tunable(TRIDI_TUNE_PCR_KERNEL) != 2 && !g_host_mapped_io;
 }
 
 tridi_status pcr_thomas2_solve(const float* a, const float* b, const float* c, const float* d, float* x, int n,

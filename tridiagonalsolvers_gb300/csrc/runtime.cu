@@ -11,9 +11,11 @@ constexpr int kMaxDevices = 64;
 DeviceInfo g_dev[kMaxDevices];
 std::mutex g_mu;
 thread_local int t_last_cuda_error = 0;
-constexpr int kTunables = 11;
+constexpr int kTunables = 12;
 int g_tunable[kTunables] = {};
 }  // namespace
+
+thread_local bool g_host_mapped_io = false;
 
 int tunable(int key) { return key >= 0 && key < kTunables ? g_tunable[key] : 0; }
 

@@ -32,6 +32,11 @@ inline cudaStream_t as_stream(tridi_stream_t s) { return reinterpret_cast<cudaSt
 // Launch-shape tunables (tridi_set_tunable); 0 means "choose automatically".
 int tunable(int key);
 
+// Set, on the calling thread, while a host-pointer launcher runs its kernels
+// on host memory that the device maps (pinned, mapped arrays): the launches
+// then read their inputs with plain loads, never with bulk or tensor copies.
+extern thread_local bool g_host_mapped_io;
+
 // Table written by the autotuner (tridi_autotune): per table (TRIDI_AUTOTUNE_*)
 // and key (log2 of the system size, or of the size bucket), the chosen value;
 // 0 where nothing was tuned.
