@@ -83,7 +83,7 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
                                      (same arithmetic and results, about twice as fast), 2 = the
                                      shared-memory kernel always */
 #define TRIDI_TUNE_DROPIN_CHUNK 9 /* host-pointer launchers: KiB of each coefficient array per pipelined chunk
-                                     (0 = 8192) */
+                                     (0 = 8192 from pinned memory, 65536 from pageable memory) */
 #define TRIDI_TUNE_PCR_KERNEL 10  /* FP32 PCR on 64..1024 unknowns: 0/1 = the two-phase kernel (rows transposed
                                      once between the register phases) with paired FP32 instructions,
                                      3 = the same on single rows, 2 = the hybrid warp kernel (the same
