@@ -229,3 +229,32 @@ def test_dropin_pinned_arrays_solved_in_place(cuda, prec, n):
     for p, v in zip((pa, pb, pc, pd), (a, b, c, d)):
         assert np.array_equal(p, np.ascontiguousarray(v).reshape(-1))
     assert tg.device_status() == 0
+
+
+@pytest.mark.parametrize("n", [2, 8, 32, 64, 512, 2048, 4096])
+def test_dropin_pinned_cr_sizes(cuda, n):
+    """cr() on pinned, mapped arrays across the system sizes (warp and block
+    shapes of the hybrid kernels reading host memory directly), against the
+    staged path bit for bit and against the FP64 oracle."""
+    import torch
+
+    from tridiagonalsolvers_gb300._lib import lib
+
+    m = 33
+    a, b, c, d = workloads.dominant(m, n, seed=5 + n)
+
+    def pinned(v):
+        return torch.from_numpy(np.ascontiguousarray(v).reshape(-1).copy()).pin_memory().numpy()
+
+    pa, pb, pc, pd = (pinned(v) for v in (a, b, c, d))
+    x_in = pinned(np.zeros(m * n, np.float32))
+    dropin.cr(pa, pb, pc, pd, x_in, n, m)
+    x_st = pinned(np.zeros(m * n, np.float32))
+    L = lib()
+    assert L.tridi_set_tunable(11, 2) == 0
+    try:
+        dropin.cr(pa, pb, pc, pd, x_st, n, m)
+    finally:
+        L.tridi_set_tunable(11, 0)
+    check_against_oracle(a, b, c, d, x_in.reshape(m, n))
+    assert np.array_equal(x_in, x_st)

@@ -9,7 +9,7 @@ import tridiagonalsolvers_gb300 as tg
 from oracle import gold
 from tridiagonalsolvers_gb300 import dropin, workloads
 
-from .parity import check_against_oracle, check_ulps_where_reference_valid, legacy_accept
+from .parity import check_against_oracle, check_ulps, check_ulps_where_reference_valid, legacy_accept
 
 pytestmark = pytest.mark.gpu
 NP = {"f32": np.float32, "f64": np.float64}
@@ -148,3 +148,29 @@ def test_pcr_gauss_wrapper_large_many_chunks(cuda):
     x = np.zeros_like(a)
     dropin.pcrGaussWrapper(a, b, c, d, x, n, m, 64)
     check_against_oracle(a, b, c, d, x)
+
+
+@pytest.mark.parametrize("n", [64, 128, 256, 512, 1024])
+def test_pcr_thomas_register_kernel_every_split(cuda, n):
+    """The register PCR-then-Thomas kernel (FP32, 64..1024 unknowns, g < n/2)
+    for every split, including partial warp tiles (m not a multiple of the
+    systems a warp tile holds) and one system: against the FP64 oracle, and
+    within a few ulp of the shared-memory kernel (TRIDI_TUNE_PCR_KERNEL = 2)."""
+    from tridiagonalsolvers_gb300._lib import lib
+
+    L = lib()
+    for m in (1, 7, 130):
+        a, b, c, d = workloads.dominant(m, n, seed=11 * n + m)
+        t = _dev(cuda, a, b, c, d)
+        g = 1
+        while g < n // 2:
+            x = tg.pcrGauss(*t, g).cpu().numpy()
+            check_against_oracle(a, b, c, d, x)
+            assert L.tridi_set_tunable(10, 2) == 0
+            try:
+                xs = tg.pcrGauss(*t, g).cpu().numpy()
+            finally:
+                L.tridi_set_tunable(10, 0)
+            check_ulps(x, xs, ulps=16)
+            g *= 2
+    assert tg.device_status() == 0
