@@ -65,6 +65,30 @@ def test_crpcr_switch_level_sweep(cuda, n, prec):
         rest *= 2
 
 
+@pytest.mark.parametrize("rest", [256, 512])
+def test_crpcr_1024_register_kernels(cuda, rest):
+    """The register CR-PCR kernels for 1024 unknowns (FP32, rest = n/4 and
+    n/2), on one system, a few, and more systems than one wave of warps
+    holds (so warps loop over tiles): against the FP64 oracle, and within a
+    few ulp of the shared-memory kernel (TRIDI_TUNE_PCR_KERNEL = 2)."""
+    from tridiagonalsolvers_gb300._lib import lib
+
+    L = lib()
+    n = 1024
+    for m in (1, 5, 2 * 152 * 3 * 2 + 3):
+        a, b, c, d = workloads.dominant(m, n, seed=13 * m + rest)
+        t = _dev(cuda, a, b, c, d)
+        x = tg.crpcr(*t, rest).cpu().numpy()
+        check_against_oracle(a, b, c, d, x)
+        assert L.tridi_set_tunable(10, 2) == 0
+        try:
+            xs = tg.crpcr(*t, rest).cpu().numpy()
+        finally:
+            L.tridi_set_tunable(10, 0)
+        check_ulps(x, xs, ulps=16)
+    assert tg.device_status() == 0
+
+
 def test_reference_driver_case(cuda):
     """The reference driver's inputs (testGeneration, 2 x 8192 after srand(1))
     checked with its own 1e-3 RMS acceptance; CR family limits n to 4096 here,

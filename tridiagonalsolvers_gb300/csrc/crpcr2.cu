@@ -33,6 +33,8 @@ constexpr int kWarps = 2;       // warps per CTA
 constexpr int kScratch = 512 + 32;  // one word array of the 512-row transpose, then x of the 512 rows (padded)
 constexpr size_t kSmem = 128 + (size_t)kWarps * kScratch * sizeof(float) + 1024 + (size_t)kWarps * 4 * kTF * 4;
 
+constexpr size_t kSmem256 = 128 + (size_t)kWarps * 3 * (256 + 32) * sizeof(float) + 1024 + (size_t)kWarps * 4 * kTF * 4;
+
 __device__ __forceinline__ int xr_index(int r) { return r + (r >> 4); }  // one pad word per 16
 
 __global__ void __launch_bounds__(kWarps * 32, 3)
@@ -164,24 +166,188 @@ __global__ void __launch_bounds__(kWarps * 32, 3)
   }
 }
 
-}  // namespace
-
-// True when the register kernel takes this FP32 call: crpcr with rest = n/2
-// at n = 1024, 16-byte aligned a..d and x, the batch within the tensor maps'
-// 32-bit row count.
-bool crpcr512_applies(const void* a, const void* b, const void* c, const void* d, const void* x, int n, long m,
-                      int stride) {
-  return n == kN && stride == 2 && aligned16(a) && aligned16(b) && aligned16(c) && aligned16(d) && aligned16(x) &&
-         m * n / 32 < (1L << 31) && tunable(TRIDI_TUNE_PCR_KERNEL) != 2 && !g_host_mapped_io;
+// One CR level of the lane's K unnormalised rows (local rows 0..K-1 of a
+// contiguous block): the odd rows 2j+1 eliminate their even neighbours (the
+// last one's right neighbour, row K of the block, is the next lane's row 0:
+// one shuffle; lane 31's has c = 0 and contributes nothing).  The K/2 new
+// rows land in (na, nb, nc, nd).
+template <int K>
+__device__ __forceinline__ void cr_level(const float (&a)[K], const float (&b)[K], const float (&c)[K],
+                                         const float (&d)[K], float (&na)[K / 2], float (&nb)[K / 2],
+                                         float (&nc)[K / 2], float (&nd)[K / 2]) {
+  const float ra = __shfl_down_sync(kFull, a[0], 1), rb = __shfl_down_sync(kFull, b[0], 1);
+  const float rc = __shfl_down_sync(kFull, c[0], 1), rd = __shfl_down_sync(kFull, d[0], 1);
+#pragma unroll
+  for (int j = 0; j < K / 2; ++j) {
+    const int q = 2 * j + 1;
+    const float aR = q + 1 < K ? a[q + 1] : ra, bR = q + 1 < K ? b[q + 1] : rb;
+    const float cR = q + 1 < K ? c[q + 1] : rc, dR = q + 1 < K ? d[q + 1] : rd;
+    const float k1 = tdiv(a[q], b[q - 1]);
+    const float k2 = tdiv(c[q], bR);
+    na[j] = -a[q - 1] * k1;
+    nb[j] = b[q] - c[q - 1] * k1 - aR * k2;
+    nc[j] = -cR * k2;
+    nd[j] = d[q] - d[q - 1] * k1 - dR * k2;
+  }
 }
 
-tridi_status crpcr512_solve(const float* a, const float* b, const float* c, const float* d, float* x, int m,
-                            cudaStream_t stream) {
+// The even rows of a CR level given x of the odd ones (xo[j] = x of row 2j+1
+// of the lane's block): x[2j] = (d - a x[2j-1] - c x[2j+1]) / b, row -1 the
+// previous lane's last odd row (zero for lane 0, whose first row has a = 0).
+template <int K>
+__device__ __forceinline__ void cr_back(const float (&a)[K], const float (&b)[K], const float (&c)[K],
+                                        const float (&d)[K], const float (&xo)[K / 2], float (&x)[K], int lane) {
+  float xprev = __shfl_up_sync(kFull, xo[K / 2 - 1], 1);
+  if (lane == 0) xprev = 0.0f;
+#pragma unroll
+  for (int j = 0; j < K / 2; ++j) {
+    x[2 * j] = (d[2 * j] - a[2 * j] * xprev - c[2 * j] * xo[j]) * rcp_approx(b[2 * j]);
+    x[2 * j + 1] = xo[j];
+    xprev = xo[j];
+  }
+}
+
+constexpr int kS256 = 256 + 32;  // the 256-row PCR's scratch per word array (one pad word per 8 rows:
+                                 // lane stride 9 words, conflict-free at every distance)
+__device__ __forceinline__ int r256_index(int r) { return r + (r >> 3); }
+
+// CR-PCR with the switch at n/4 for 1024 unknowns: two CR levels inside the
+// lane (32 -> 16 -> 8 rows), PCR on the 256 rows left (distances 1, 2, 4
+// inside the lane over shuffles, 8 .. 64 through the warp's scratch, the
+// closing pairs (r, r + 128) over one xor-16 shuffle), the two back
+// substitutions in the lane, 16-byte stores.
+__global__ void __launch_bounds__(kWarps * 32, 3)
+    crpcr256_kernel(HybridParams p, const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb,
+                    const __grid_constant__ CUtensorMap mc, const __grid_constant__ CUtensorMap md) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem) + warp;
+  float* sw = reinterpret_cast<float*>(smem + 128) + (size_t)warp * 3 * kS256;
+  const uint32_t base = smem_addr(smem);
+  const uint32_t ring = (base + 128 + kWarps * 3 * kS256 * (uint32_t)sizeof(float) + 1023) & ~1023u;
+  float* buf = reinterpret_cast<float*>(smem + (ring - base)) + (size_t)warp * 4 * kTF;
+  float* gx = static_cast<float*>(p.x);
+  const long tiles = p.m;
+  const long first = (long)blockIdx.x * kWarps + warp;
+  const long step = (long)gridDim.x * kWarps;
+  if (lane == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  __syncwarp();
+  const auto issue = [&](long tile) {
+    const int row = (int)(tile * (kTF / 32));
+    mbar_arrive_expect_tx(bar, 4 * kTF * sizeof(float));
+    tma_load_2d(buf + 0 * kTF, &ma, 0, row, bar);
+    tma_load_2d(buf + 1 * kTF, &mb, 0, row, bar);
+    tma_load_2d(buf + 2 * kTF, &mc, 0, row, bar);
+    tma_load_2d(buf + 3 * kTF, &md, 0, row, bar);
+  };
+  if (lane == 0 && first < tiles) issue(first);
+  int chunk[kR / 4];
+#pragma unroll
+  for (int q = 0; q < kR / 4; ++q) {
+    const int c = lane * (kR / 4) + q, row = c >> 3;
+    chunk[q] = row * 32 + (((c & 7) ^ (row & 7)) << 2);
+  }
+  float* sa = sw;
+  float* sc = sw + kS256;
+  float* sd = sw + 2 * kS256;
+  int k = 0;
+  for (long tile = first; tile < tiles; tile += step, ++k) {
+    if (!mbar_wait(bar, k & 1, p.status)) break;
+    float v[4][kR];
+#pragma unroll
+    for (int arr = 0; arr < 4; ++arr)
+#pragma unroll
+      for (int q = 0; q < kR / 4; ++q) {
+        const float4 f = *reinterpret_cast<const float4*>(buf + arr * kTF + chunk[q]);
+        v[arr][4 * q] = f.x; v[arr][4 * q + 1] = f.y; v[arr][4 * q + 2] = f.z; v[arr][4 * q + 3] = f.w;
+      }
+    fence_proxy_async_smem();
+    __syncwarp();
+    if (lane == 0 && tile + step < tiles) issue(tile + step);
+    if (lane == 0) v[0][0] = 0.0f;
+    if (lane == 31) v[2][kR - 1] = 0.0f;
+    // ---- two CR levels inside the lane: 32 -> 16 -> 8 rows ----
+    float a1[16], b1[16], c1[16], d1[16];
+    cr_level<32>(v[0], v[1], v[2], v[3], a1, b1, c1, d1);
+    float a2[8], b2[8], c2[8], d2[8];
+    cr_level<16>(a1, b1, c1, d1, a2, b2, c2, d2);
+    // ---- PCR on the 256 rows: lane t holds rows 8t .. 8t+7, normalised ----
+    NR w[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const float ib = rcp_approx(b2[j]);
+      w[j] = NR{a2[j] * ib, c2[j] * ib, d2[j] * ib};
+    }
+    phase_a_step<1, 32, 8>(w);
+    phase_a_step<2, 32, 8>(w);
+    phase_a_step<4, 32, 8>(w);
+#pragma unroll
+    for (int D = 8; D <= 64; D *= 2) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int r = 8 * lane + j;
+        sa[r256_index(r)] = w[j].a;
+        sc[r256_index(r)] = w[j].c;
+        sd[r256_index(r)] = w[j].d;
+      }
+      __syncwarp();
+      NR o[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int r = 8 * lane + j;
+        // a neighbour beyond the system's ends: the row itself (its coupling there is exactly zero)
+        const int il = r - D >= 0 ? r - D : r, ir = r + D < 256 ? r + D : r;
+        const NR L{sa[r256_index(il)], sc[r256_index(il)], sd[r256_index(il)]};
+        const NR Rr{sa[r256_index(ir)], sc[r256_index(ir)], sd[r256_index(ir)]};
+        o[j] = step_both(w[j], L, Rr);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < 8; ++j) w[j] = o[j];
+    }
+    // ---- closing 2x2 systems (r, r + 128): lanes t and t ^ 16, same slot ----
+    float x2[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const NR pr = shfl_xor_nr(w[j], 16);
+      const NR& u = lane < 16 ? w[j] : pr;  // row r
+      const NR& l = lane < 16 ? pr : w[j];  // row r + 128
+      const float xu = (u.d - u.c * l.d) * rcp_approx(fmaf(-u.c, l.a, 1.0f));
+      x2[j] = lane < 16 ? xu : fmaf(-l.a, xu, l.d);
+    }
+    // ---- CR back substitution: 8 -> 16 -> 32 rows ----
+    float x1[16], x[kR];
+    cr_back<16>(a1, b1, c1, d1, x2, x1, lane);
+    cr_back<32>(v[0], v[1], v[2], v[3], x1, x, lane);
+    if (tile < p.m) {
+      float4* dst = reinterpret_cast<float4*>(gx + tile * kN + kR * lane);
+#pragma unroll
+      for (int q = 0; q < kR / 4; ++q) dst[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+    }
+  }
+}
+
+}  // namespace
+
+// True when a register kernel takes this FP32 call: crpcr with rest = n/2
+// or n/4 at n = 1024, 16-byte aligned a..d and x, the batch within the tensor
+// maps' 32-bit row count.
+bool crpcr1024_applies(const void* a, const void* b, const void* c, const void* d, const void* x, int n, long m,
+                       int stride) {
+  return n == kN && (stride == 2 || stride == 4) && aligned16(a) && aligned16(b) && aligned16(c) && aligned16(d) &&
+         aligned16(x) && m * n / 32 < (1L << 31) && tunable(TRIDI_TUNE_PCR_KERNEL) != 2 && !g_host_mapped_io;
+}
+
+tridi_status crpcr1024_solve(const float* a, const float* b, const float* c, const float* d, float* x, int m,
+                             int stride, cudaStream_t stream) {
   const DeviceInfo* dev = current_device();
   if (!dev) return TRIDI_ERROR_CUDA;
   HybridParams p{};
   p.a = a; p.b = b; p.c = c; p.d = d; p.x = x;
-  p.n = kN; p.m = m; p.stride = 2;
+  p.n = kN; p.m = m; p.stride = stride;
   p.status = dev->status;
   const uint64_t rows = (uint64_t)m * kN / 32;
   CUtensorMap tma, tmb, tmc, tmd;
@@ -190,16 +356,18 @@ tridi_status crpcr512_solve(const float* a, const float* b, const float* c, cons
       !make_tensor_map_2d(&tmc, c, 32, rows, 128, 32, kR, true) ||
       !make_tensor_map_2d(&tmd, d, 32, rows, 128, 32, kR, true))
     return cuda_status(cudaErrorInvalidValue);
-  if (kSmem > (size_t)dev->max_smem_optin) return TRIDI_ERROR_UNSUPPORTED_SIZE;
-  cudaError_t e = cudaFuncSetAttribute(crpcr512_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+  const auto kern = stride == 2 ? crpcr512_kernel : crpcr256_kernel;
+  const size_t smem = stride == 2 ? kSmem : kSmem256;
+  if (smem > (size_t)dev->max_smem_optin) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e);
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, crpcr512_kernel, kWarps * 32, kSmem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
   if (e != cudaSuccess) return cuda_status(e);
   if (per_sm < 1) per_sm = 1;
   long grid = (long)per_sm * dev->sm_count;
   if (grid * kWarps > m) grid = (m + kWarps - 1) / kWarps;
-  crpcr512_kernel<<<(unsigned)grid, kWarps * 32, kSmem, stream>>>(p, tma, tmb, tmc, tmd);
+  kern<<<(unsigned)grid, kWarps * 32, smem, stream>>>(p, tma, tmb, tmc, tmd);
   return cuda_status(cudaGetLastError());
 }
 
