@@ -65,17 +65,19 @@ def test_crpcr_switch_level_sweep(cuda, n, prec):
         rest *= 2
 
 
-@pytest.mark.parametrize("rest", [256, 512])
+@pytest.mark.parametrize("rest", [2, 4, 8, 16, 32, 64, 128, 256, 512])
 def test_crpcr_1024_register_kernels(cuda, rest):
-    """The register CR-PCR kernels for 1024 unknowns (FP32, rest = n/4 and
-    n/2), on one system, a few, and more systems than one wave of warps
-    holds (so warps loop over tiles): against the FP64 oracle, and within a
-    few ulp of the shared-memory kernel (TRIDI_TUNE_PCR_KERNEL = 2)."""
+    """The register CR-PCR kernels for 1024 unknowns (FP32, every switch
+    level; rest 2 is cr), on one system, a few, and more systems than one
+    wave of warps holds (so warps loop over tiles): against the FP64 oracle,
+    and against the shared-memory kernel (TRIDI_TUNE_PCR_KERNEL = 2): bit for
+    bit at rest 2 (the same CR arithmetic), within a few ulp above (the
+    register kernels' PCR works on normalised rows)."""
     from tridiagonalsolvers_gb300._lib import lib
 
     L = lib()
     n = 1024
-    for m in (1, 5, 2 * 152 * 3 * 2 + 3):
+    for m in (1, 5, 2 * 152 * 4 * 2 + 3):
         a, b, c, d = workloads.dominant(m, n, seed=13 * m + rest)
         t = _dev(cuda, a, b, c, d)
         x = tg.crpcr(*t, rest).cpu().numpy()
@@ -85,7 +87,11 @@ def test_crpcr_1024_register_kernels(cuda, rest):
             xs = tg.crpcr(*t, rest).cpu().numpy()
         finally:
             L.tridi_set_tunable(10, 0)
-        check_ulps(x, xs, ulps=16)
+        if rest == 2:
+            assert np.array_equal(x, xs)
+            assert np.array_equal(x, tg.cr(*t).cpu().numpy())
+        else:
+            check_ulps(x, xs, ulps=16)
     assert tg.device_status() == 0
 
 

@@ -1,19 +1,31 @@
-// CR-PCR with the switch at half the system ("crpcr" with restSystemSize =
-// n/2, crpcr_kernel.cu:1-148, crpcr_app.cu:5) for FP32 systems of 1024
-// unknowns, in registers: one CR level, PCR on the 512-row intermediate
-// system, the CR back substitution.
+// CR-PCR for FP32 systems of 1024 unknowns in registers, one system a warp
+// (32 contiguous rows a lane, loaded by TMA into the warp's buffer): every
+// switch level of "crpcr" (restSystemSize 2 .. 512, crpcr_kernel.cu:1-148,
+// crpcr_app.cu:5) and, at rest 2, "cr" (cr_kernel.cu, cr_app.cu:4).
 //
-// A warp holds one system, 32 contiguous rows a lane (the 1024-row tile of
-// pcr_twophase.cuh).  The CR level eliminates the even rows from the odd ones
-// inside the lane (the last odd row's right neighbour is the next lane's
-// first row, one shuffle): lane t keeps the intermediate rows 16t .. 16t+15
-// (original rows 32t + 2j + 1) as normalised 3-word rows -- exactly the
-// 512-row layout of the two-phase PCR (16 rows a lane, one system a warp), so
-// its phase A, transpose, phase B and closing 2x2 systems run unchanged and
-// leave x of intermediate row t + 32s in lane t.  Those 512 values go through
-// the warp's scratch once (padded so the lane-contiguous reads hit distinct
-// banks), each lane forms its 16 even rows' x from its own coefficients, and
-// writes its 32 unknowns with 16-byte stores.
+// crpcr_lanes_kernel<LEV> (rest = 1024 / 2^LEV, LEV = 2 .. 9): the first five
+// CR levels run inside the lane (32 -> 16 -> 8 -> 4 -> 2 -> 1 rows; each level's
+// last odd row takes its right neighbour from the next lane over one
+// shuffle), the levels past five between lanes (lane strides 1, 2, 4, 8).
+// PCR on the rows left: distances below the rows a lane holds inside the
+// lane, the others between lanes (the neighbour at distance K2 ld is lane
+// t -/+ ld, same slot), the closing 2x2 systems between lanes t and t ^ 16.
+// The back substitutions retrace the levels from the coefficients each lane
+// kept in registers; the lane's 32 unknowns leave in 16-byte stores.  No
+// shared memory but the TMA buffer.  At rest 2 the closing solve is CR's own
+// (unnormalised rows), so cr here rounds exactly like every other CR kernel
+// of the library.
+//
+// crpcr512_kernel (rest 512): one CR level inside the lane leaves lane t the
+// intermediate rows 16t .. 16t+15 as normalised 3-word rows -- exactly the
+// 512-row layout of the two-phase PCR (pcr_twophase.cuh, 16 rows a lane, one
+// system a warp), so its phase A, transpose, phase B and closing 2x2 systems
+// run unchanged and leave x of intermediate row t + 32s in lane t.  Those
+// 512 values go through the warp's scratch once (padded so the
+// lane-contiguous reads hit distinct banks), each lane forms its 16 even
+// rows' x from its own coefficients, and writes its 32 unknowns.  (The lanes
+// design at rest 512 -- 16 rows a lane, four PCR steps between lanes with 16
+// rows each -- measured 64 % of HBM against this kernel's 80 %.)
 #include "hybrid.cuh"
 #include "pcr_twophase.cuh"
 #include "runtime.h"
@@ -32,8 +44,6 @@ constexpr int kTF = kN;         // values of one array in a warp tile (one syste
 constexpr int kWarps = 2;       // warps per CTA
 constexpr int kScratch = 512 + 32;  // one word array of the 512-row transpose, then x of the 512 rows (padded)
 constexpr size_t kSmem = 128 + (size_t)kWarps * kScratch * sizeof(float) + 1024 + (size_t)kWarps * 4 * kTF * 4;
-
-constexpr size_t kSmem256 = 128 + (size_t)kWarps * 3 * (256 + 32) * sizeof(float) + 1024 + (size_t)kWarps * 4 * kTF * 4;
 
 __device__ __forceinline__ int xr_index(int r) { return r + (r >> 4); }  // one pad word per 16
 
@@ -207,24 +217,134 @@ __device__ __forceinline__ void cr_back(const float (&a)[K], const float (&b)[K]
   }
 }
 
-constexpr int kS256 = 256 + 32;  // the 256-row PCR's scratch per word array (one pad word per 8 rows:
-                                 // lane stride 9 words, conflict-free at every distance)
-__device__ __forceinline__ int r256_index(int r) { return r + (r >> 3); }
+// PCR step between lanes: lane t holds rows K2 t + j, so the neighbours at
+// distance K2 ld are lanes t -/+ ld in the same slot.  Lanes whose neighbour
+// lies beyond the system's ends receive their own row from the shuffle: the
+// coupling there is exactly zero.
+template <int K2>
+__device__ __forceinline__ void lane_step(NR (&w)[K2], int ld) {
+#pragma unroll
+  for (int j = 0; j < K2; ++j) {
+    const NR L{__shfl_up_sync(kFull, w[j].a, ld), __shfl_up_sync(kFull, w[j].c, ld),
+               __shfl_up_sync(kFull, w[j].d, ld)};
+    const NR Rr{__shfl_down_sync(kFull, w[j].a, ld), __shfl_down_sync(kFull, w[j].c, ld),
+                __shfl_down_sync(kFull, w[j].d, ld)};
+    w[j] = step_both(w[j], L, Rr);
+  }
+}
 
-// CR-PCR with the switch at n/4 for 1024 unknowns: two CR levels inside the
-// lane (32 -> 16 -> 8 rows), PCR on the 256 rows left (distances 1, 2, 4
-// inside the lane over shuffles, 8 .. 64 through the warp's scratch, the
-// closing pairs (r, r + 128) over one xor-16 shuffle), the two back
-// substitutions in the lane, 16-byte stores.
-__global__ void __launch_bounds__(kWarps * 32, 3)
-    crpcr256_kernel(HybridParams p, const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb,
-                    const __grid_constant__ CUtensorMap mc, const __grid_constant__ CUtensorMap md) {
+// PCR on the rows left by the CR levels: lane t holds rows K2 t .. K2 t + K2 - 1
+// (unnormalised) of the 32 K2 rows, or, after CR levels between lanes
+// (LD0 = 2^levels > 1, K2 = 1), only the lanes t = LD0 j + LD0 - 1 hold a row
+// (row j of 32 / LD0).  Distances below K2 run inside the lane, the others
+// between lanes (lane distances LD0 .. 8), then the closing 2x2 systems
+// pair lane t with lane t ^ 16 in the same slot.  x of the lane's rows out
+// (meaningless on lanes that hold no row).
+template <int K2, int LD0>
+__device__ __forceinline__ void pcr_lanes(const float (&a)[K2], const float (&b)[K2], const float (&c)[K2],
+                                          const float (&d)[K2], float (&x)[K2], int lane) {
+  NR w[K2];
+#pragma unroll
+  for (int j = 0; j < K2; ++j) {
+    const float ib = rcp_approx(b[j]);
+    w[j] = NR{a[j] * ib, c[j] * ib, d[j] * ib};
+  }
+  if constexpr (K2 >= 2) phase_a_step<1, 32, K2>(w);
+  if constexpr (K2 >= 4) phase_a_step<2, 32, K2>(w);
+  if constexpr (K2 >= 8) phase_a_step<4, 32, K2>(w);
+  if constexpr (K2 >= 16) phase_a_step<8, 32, K2>(w);
+#pragma unroll
+  for (int ld = LD0; ld < 16; ld *= 2) lane_step<K2>(w, ld);
+#pragma unroll
+  for (int j = 0; j < K2; ++j) {
+    const NR pr = shfl_xor_nr(w[j], 16);
+    const NR& u = lane < 16 ? w[j] : pr;  // row r
+    const NR& l = lane < 16 ? pr : w[j];  // row r + 16 K2 (r + 16 / LD0 between lanes)
+    const float xu = (u.d - u.c * l.d) * rcp_approx(fmaf(-u.c, l.a, 1.0f));
+    x[j] = lane < 16 ? xu : fmaf(-l.a, xu, l.d);
+  }
+}
+
+// L2 CR levels between lanes on a 32-row system held one row a lane (row t in
+// lane t), the PCR of the 32 / 2^L2 rows left, and the back substitutions.
+// Level i (lane stride s = 2^i) leaves the rows of lanes t with
+// (t + 1) mod 2s = 0, each from its neighbours t -/+ s; every lane computes
+// (the warp stays converged) and keeps the row it held at each level for the
+// back substitution, where the lanes with (t + 1) mod 2s = s take x from
+// lanes t -/+ s.  Active rows only ever read active rows; the last row's
+// c = 0 zeroes the neighbour that lane 31 receives from itself, and the
+// first row's a = 0 the one that lane s - 1 receives from itself.
+template <int L2>
+__device__ __forceinline__ float cr_cross(float a, float b, float c, float d, int lane) {
+  float la[L2], lb[L2], lc[L2], ld[L2];
+#pragma unroll
+  for (int i = 0; i < L2; ++i) {
+    const int s = 1 << i;
+    const float aL = __shfl_up_sync(kFull, a, s), bL = __shfl_up_sync(kFull, b, s);
+    const float cL = __shfl_up_sync(kFull, c, s), dL = __shfl_up_sync(kFull, d, s);
+    const float aR = __shfl_down_sync(kFull, a, s), bR = __shfl_down_sync(kFull, b, s);
+    const float cR = __shfl_down_sync(kFull, c, s), dR = __shfl_down_sync(kFull, d, s);
+    la[i] = a; lb[i] = b; lc[i] = c; ld[i] = d;
+    const float k1 = tdiv(a, bL);
+    const float k2 = tdiv(c, bR);
+    a = -aL * k1;
+    b = b - cL * k1 - aR * k2;
+    c = -cR * k2;
+    d = d - dL * k1 - dR * k2;
+  }
+  float x = 0.0f;
+  if constexpr (L2 == 4) {
+    // two rows left (lanes 15 and 31): CR's closing 2x2 solve on the
+    // unnormalised rows, so that cr here rounds like every other CR kernel
+    const Row<float> r1{__shfl_sync(kFull, a, 15), __shfl_sync(kFull, b, 15), __shfl_sync(kFull, c, 15),
+                        __shfl_sync(kFull, d, 15)};
+    const Row<float> r2{__shfl_sync(kFull, a, 31), __shfl_sync(kFull, b, 31), __shfl_sync(kFull, c, 31),
+                        __shfl_sync(kFull, d, 31)};
+    if (lane == 15) x = solve2_upper(r1, r2);
+    if (lane == 31) x = solve2_lower(r1, r2);
+  } else {
+    const float ta[1] = {a}, tb[1] = {b}, tc[1] = {c}, td[1] = {d};
+    float xt[1];
+    pcr_lanes<1, (1 << L2)>(ta, tb, tc, td, xt, lane);
+    if (((lane + 1) & ((1 << L2) - 1)) == 0) x = xt[0];
+  }
+#pragma unroll
+  for (int i = L2 - 1; i >= 0; --i) {
+    const int s = 1 << i;
+    const float xL = __shfl_up_sync(kFull, x, s), xR = __shfl_down_sync(kFull, x, s);
+    if (((lane + 1) & (2 * s - 1)) == s) x = (ld[i] - la[i] * xL - lc[i] * xR) * rcp_approx(lb[i]);
+  }
+  return x;
+}
+
+// LEV CR levels down from the lane's K rows (the levels past K = 1 between
+// lanes), the PCR, and the back substitutions up again.
+template <int K, int LEV>
+__device__ __forceinline__ void cr_solve(const float (&a)[K], const float (&b)[K], const float (&c)[K],
+                                         const float (&d)[K], float (&x)[K], int lane) {
+  float na[K / 2], nb[K / 2], nc[K / 2], nd[K / 2], xo[K / 2];
+  cr_level<K>(a, b, c, d, na, nb, nc, nd);
+  if constexpr (LEV == 1) pcr_lanes<K / 2, 1>(na, nb, nc, nd, xo, lane);
+  else if constexpr (K == 2) xo[0] = cr_cross<LEV - 1>(na[0], nb[0], nc[0], nd[0], lane);
+  else cr_solve<K / 2, LEV - 1>(na, nb, nc, nd, xo, lane);
+  cr_back<K>(a, b, c, d, xo, x, lane);
+}
+
+constexpr size_t kSmemLanes = 128 + 1024 + (size_t)kWarps * 4 * kTF * 4;
+
+// CR-PCR with the switch at 1024 / 2^LEV for 1024 unknowns, in registers and
+// shuffles (the file header gives the scheme).  Four CTAs of two warps an SM
+// (at most 255 registers: none spill); three or five to six measured the same
+// or slower.
+template <int LEV>
+__global__ void __launch_bounds__(kWarps * 32, 4)
+    crpcr_lanes_kernel(HybridParams p, const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb,
+                       const __grid_constant__ CUtensorMap mc, const __grid_constant__ CUtensorMap md) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem) + warp;
-  float* sw = reinterpret_cast<float*>(smem + 128) + (size_t)warp * 3 * kS256;
   const uint32_t base = smem_addr(smem);
-  const uint32_t ring = (base + 128 + kWarps * 3 * kS256 * (uint32_t)sizeof(float) + 1023) & ~1023u;
+  const uint32_t ring = (base + 128 + 1023) & ~1023u;
   float* buf = reinterpret_cast<float*>(smem + (ring - base)) + (size_t)warp * 4 * kTF;
   float* gx = static_cast<float*>(p.x);
   const long tiles = p.m;
@@ -250,9 +370,6 @@ __global__ void __launch_bounds__(kWarps * 32, 3)
     const int c = lane * (kR / 4) + q, row = c >> 3;
     chunk[q] = row * 32 + (((c & 7) ^ (row & 7)) << 2);
   }
-  float* sa = sw;
-  float* sc = sw + kS256;
-  float* sd = sw + 2 * kS256;
   int k = 0;
   for (long tile = first; tile < tiles; tile += step, ++k) {
     if (!mbar_wait(bar, k & 1, p.status)) break;
@@ -269,76 +386,43 @@ __global__ void __launch_bounds__(kWarps * 32, 3)
     if (lane == 0 && tile + step < tiles) issue(tile + step);
     if (lane == 0) v[0][0] = 0.0f;
     if (lane == 31) v[2][kR - 1] = 0.0f;
-    // ---- two CR levels inside the lane: 32 -> 16 -> 8 rows ----
-    float a1[16], b1[16], c1[16], d1[16];
-    cr_level<32>(v[0], v[1], v[2], v[3], a1, b1, c1, d1);
-    float a2[8], b2[8], c2[8], d2[8];
-    cr_level<16>(a1, b1, c1, d1, a2, b2, c2, d2);
-    // ---- PCR on the 256 rows: lane t holds rows 8t .. 8t+7, normalised ----
-    NR w[8];
+    float x[kR];
+    cr_solve<kR, LEV>(v[0], v[1], v[2], v[3], x, lane);
+    float4* dst = reinterpret_cast<float4*>(gx + tile * kN + kR * lane);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const float ib = rcp_approx(b2[j]);
-      w[j] = NR{a2[j] * ib, c2[j] * ib, d2[j] * ib};
-    }
-    phase_a_step<1, 32, 8>(w);
-    phase_a_step<2, 32, 8>(w);
-    phase_a_step<4, 32, 8>(w);
-#pragma unroll
-    for (int D = 8; D <= 64; D *= 2) {
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int r = 8 * lane + j;
-        sa[r256_index(r)] = w[j].a;
-        sc[r256_index(r)] = w[j].c;
-        sd[r256_index(r)] = w[j].d;
-      }
-      __syncwarp();
-      NR o[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int r = 8 * lane + j;
-        // a neighbour beyond the system's ends: the row itself (its coupling there is exactly zero)
-        const int il = r - D >= 0 ? r - D : r, ir = r + D < 256 ? r + D : r;
-        const NR L{sa[r256_index(il)], sc[r256_index(il)], sd[r256_index(il)]};
-        const NR Rr{sa[r256_index(ir)], sc[r256_index(ir)], sd[r256_index(ir)]};
-        o[j] = step_both(w[j], L, Rr);
-      }
-      __syncwarp();
-#pragma unroll
-      for (int j = 0; j < 8; ++j) w[j] = o[j];
-    }
-    // ---- closing 2x2 systems (r, r + 128): lanes t and t ^ 16, same slot ----
-    float x2[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const NR pr = shfl_xor_nr(w[j], 16);
-      const NR& u = lane < 16 ? w[j] : pr;  // row r
-      const NR& l = lane < 16 ? pr : w[j];  // row r + 128
-      const float xu = (u.d - u.c * l.d) * rcp_approx(fmaf(-u.c, l.a, 1.0f));
-      x2[j] = lane < 16 ? xu : fmaf(-l.a, xu, l.d);
-    }
-    // ---- CR back substitution: 8 -> 16 -> 32 rows ----
-    float x1[16], x[kR];
-    cr_back<16>(a1, b1, c1, d1, x2, x1, lane);
-    cr_back<32>(v[0], v[1], v[2], v[3], x1, x, lane);
-    if (tile < p.m) {
-      float4* dst = reinterpret_cast<float4*>(gx + tile * kN + kR * lane);
-#pragma unroll
-      for (int q = 0; q < kR / 4; ++q) dst[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
-    }
+    for (int q = 0; q < kR / 4; ++q) dst[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
   }
+}
+
+using TileKernel = void (*)(HybridParams, CUtensorMap, CUtensorMap, CUtensorMap, CUtensorMap);
+
+// One warp a system, as many CTAs of two warps as fit on every SM (the
+// warps then loop over the batch).
+tridi_status launch_tiles(TileKernel kern, size_t smem, const HybridParams& p, const CUtensorMap* tm,
+                          const DeviceInfo* dev, cudaStream_t stream) {
+  if (smem > (size_t)dev->max_smem_optin) return TRIDI_ERROR_UNSUPPORTED_SIZE;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_status(e);
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (per_sm < 1) per_sm = 1;
+  long grid = (long)per_sm * dev->sm_count;
+  if (grid * kWarps > p.m) grid = (p.m + kWarps - 1) / kWarps;
+  kern<<<(unsigned)grid, kWarps * 32, smem, stream>>>(p, tm[0], tm[1], tm[2], tm[3]);
+  return cuda_status(cudaGetLastError());
 }
 
 }  // namespace
 
-// True when a register kernel takes this FP32 call: crpcr with rest = n/2
-// or n/4 at n = 1024, 16-byte aligned a..d and x, the batch within the tensor
-// maps' 32-bit row count.
+// True when a register kernel takes this FP32 call: cr, or crpcr at any
+// switch level (stride = n / rest = 2 .. 512), at n = 1024, 16-byte aligned
+// a..d and x, the batch within the tensor maps' 32-bit row count.
 bool crpcr1024_applies(const void* a, const void* b, const void* c, const void* d, const void* x, int n, long m,
                        int stride) {
-  return n == kN && (stride == 2 || stride == 4) && aligned16(a) && aligned16(b) && aligned16(c) && aligned16(d) &&
-         aligned16(x) && m * n / 32 < (1L << 31) && tunable(TRIDI_TUNE_PCR_KERNEL) != 2 && !g_host_mapped_io;
+  return n == kN && stride >= 2 && stride <= 512 && is_pow2(stride) && aligned16(a) && aligned16(b) &&
+         aligned16(c) && aligned16(d) && aligned16(x) && m * n / 32 < (1L << 31) &&
+         tunable(TRIDI_TUNE_PCR_KERNEL) != 2 && !g_host_mapped_io;
 }
 
 tridi_status crpcr1024_solve(const float* a, const float* b, const float* c, const float* d, float* x, int m,
@@ -356,19 +440,18 @@ tridi_status crpcr1024_solve(const float* a, const float* b, const float* c, con
       !make_tensor_map_2d(&tmc, c, 32, rows, 128, 32, kR, true) ||
       !make_tensor_map_2d(&tmd, d, 32, rows, 128, 32, kR, true))
     return cuda_status(cudaErrorInvalidValue);
-  const auto kern = stride == 2 ? crpcr512_kernel : crpcr256_kernel;
-  const size_t smem = stride == 2 ? kSmem : kSmem256;
-  if (smem > (size_t)dev->max_smem_optin) return TRIDI_ERROR_UNSUPPORTED_SIZE;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return cuda_status(e);
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
-  if (e != cudaSuccess) return cuda_status(e);
-  if (per_sm < 1) per_sm = 1;
-  long grid = (long)per_sm * dev->sm_count;
-  if (grid * kWarps > m) grid = (m + kWarps - 1) / kWarps;
-  kern<<<(unsigned)grid, kWarps * 32, smem, stream>>>(p, tma, tmb, tmc, tmd);
-  return cuda_status(cudaGetLastError());
+  const CUtensorMap tm[4] = {tma, tmb, tmc, tmd};
+  switch (stride) {
+    case 2: return launch_tiles(crpcr512_kernel, kSmem, p, tm, dev, stream);
+    case 4: return launch_tiles(crpcr_lanes_kernel<2>, kSmemLanes, p, tm, dev, stream);
+    case 8: return launch_tiles(crpcr_lanes_kernel<3>, kSmemLanes, p, tm, dev, stream);
+    case 16: return launch_tiles(crpcr_lanes_kernel<4>, kSmemLanes, p, tm, dev, stream);
+    case 32: return launch_tiles(crpcr_lanes_kernel<5>, kSmemLanes, p, tm, dev, stream);
+    case 64: return launch_tiles(crpcr_lanes_kernel<6>, kSmemLanes, p, tm, dev, stream);
+    case 128: return launch_tiles(crpcr_lanes_kernel<7>, kSmemLanes, p, tm, dev, stream);
+    case 256: return launch_tiles(crpcr_lanes_kernel<8>, kSmemLanes, p, tm, dev, stream);
+    default: return launch_tiles(crpcr_lanes_kernel<9>, kSmemLanes, p, tm, dev, stream);
+  }
 }
 
 }  // namespace tridi

@@ -1,6 +1,7 @@
 // Launch logic and C-ABI entry points of the bank-conflict-free CR: the
-// register kernels of hybrid.cu by default (the same arithmetic, results
-// bit-identical to the shared-memory kernel, about twice its speed), the
+// register kernels of hybrid.cu and crpcr2.cu by default (the same CR
+// arithmetic, results bit-identical to the shared-memory kernel for crNBC,
+// within a few ulp for crpcrNBC, about twice its speed), the
 // shared-memory CR of nbc.cuh on request (TRIDI_TUNE_NBC_KERNEL = 2) or where
 // the register kernel has no shape.  Replaces the device work of crNBC()
 // (crNBC.cu:123), crNBC32() (crNBC32banks.cu:123) and crpcrNBC()
@@ -22,8 +23,9 @@ tridi_status solve_nbc(const T* a, const T* b, const T* c, const T* d, T* x, int
   if (!is_pow2(n) || n < 2 || n > nmax) return TRIDI_ERROR_UNSUPPORTED_SIZE;
   if (!is_pow2(rest) || rest < 2 || rest > (n > 2 ? n / 2 : 2)) return TRIDI_ERROR_UNSUPPORTED_SIZE;
   if (tunable(TRIDI_TUNE_NBC_KERNEL) != 2) {
-    // the register kernels: the same arithmetic (bit-identical results), no
-    // shared-memory bank traffic but conflict-free 16-byte loads of the ring
+    // the register kernels: the same CR arithmetic (bit-identical results at
+    // rest 2; the PCR of crpcr's register kernels at 1024 unknowns works on
+    // normalised rows, a few ulp apart), no shared-memory bank traffic
     tridi_status st;
     if constexpr (sizeof(T) == 4)
       st = rest == 2 ? tridi_cr_f32(a, b, c, d, x, n, m, stream) : tridi_crpcr_f32(a, b, c, d, x, n, m, rest, stream);

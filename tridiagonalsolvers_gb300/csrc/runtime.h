@@ -49,7 +49,7 @@ long ragged_team_max_rows();
 bool pcr_thomas2_applies(const void* a, const void* b, const void* c, const void* d, int n, long m, int g);
 tridi_status pcr_thomas2_solve(const float* a, const float* b, const float* c, const float* d, float* x, int n,
                                int m, int g, cudaStream_t stream);
-// CR-PCR with the switch at n/2 or n/4 for 1024 unknowns, in registers
+// cr and crpcr at every switch level for 1024 unknowns, in registers
 // (crpcr2.cu); stride = n / rest.
 bool crpcr1024_applies(const void* a, const void* b, const void* c, const void* d, const void* x, int n, long m,
                        int stride);
