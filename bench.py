@@ -518,7 +518,9 @@ def run_gpu(args):
                             "reads and writes in place over the host link (no staging copies)"},
             "e2e_pageable": {"value": world * unknowns / e2e_pg_s, "unit": "unknowns/s",
                              "h2d_bytes_per_step": 4 * unknowns * 4, "d2h_bytes_per_step": unknowns * 4,
-                             "path": "the same drop-in from ordinary (pageable) numpy arrays"},
+                             "path": "the same drop-in from ordinary (pageable) numpy arrays, " + (
+                                 "which the solver reads and writes in place through the host's page tables"
+                                 if lib.tridi_dropin_pageable_in_place() else "staged through device memory")},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": profile_traffic(), "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": BYTES_PER_UNKNOWN * unknowns},

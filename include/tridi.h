@@ -90,8 +90,10 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
                                      algorithm throughout; results differ in rounding only) */
 #define TRIDI_TUNE_DROPIN_MAPPED 11 /* host-pointer launchers (cr, pcr, crpcr, crNBC, crNBC32, crpcrNBC):
                                      0/1 = arrays that are pinned and mapped into the device's address
-                                     space are read and written in place by the solver (no staging
-                                     copies), 2 = always staged through device memory */
+                                     space, or ordinary pageable arrays on a device that reaches them
+                                     through the host's page tables, are read and written in place by
+                                     the solver (no staging copies), 2 = always staged through device
+                                     memory, 3 = in place for pinned arrays only */
 tridi_status tridi_set_tunable(int key, int value);
 int tridi_get_tunable(int key);
 

@@ -92,6 +92,11 @@ tridi_status tridi_dropin_solve_f32(int algo, const float *a, const float *b, co
                                     float *x, int system_size, int num_systems, int param);
 tridi_status tridi_dropin_solve_f64(int algo, const double *a, const double *b, const double *c,
                                     const double *d, double *x, int system_size, int num_systems, int param);
+/* 1 when the current device reads and writes ordinary pageable host memory
+   through the host's own page tables (Grace-class hosts), so the launchers
+   above solve malloc'd arrays in place instead of staging them; else 0.
+   (TRIDI_TUNE_DROPIN_MAPPED, tridi.h, selects the path.) */
+int tridi_dropin_pageable_in_place(void);
 /* Frees the persistent drop-in workspace of the current device. */
 tridi_status tridi_dropin_release(void);
 

@@ -157,7 +157,14 @@ def test_dropin_matches_device_path(cuda, name, prec):
         assert np.array_equal(u, v)
     dev_fn = {"cr": tg.cr, "pcr": tg.pcr, "crNBC": tg.crNBC, "crNBC32": tg.crNBC32}[name]
     xd = dev_fn(*_dev(cuda, a, b, c, d)).cpu().numpy()
-    assert np.array_equal(x, xd)
+    from tridiagonalsolvers_gb300._lib import lib
+
+    if name == "pcr" and prec == "f32" and lib().tridi_dropin_pageable_in_place():
+        # solved in place from the pageable arrays: the hybrid kernel's PCR (plain
+        # loads) against the two-phase PCR kernel of the device path
+        check_ulps(x, xd, ulps=64)
+    else:
+        assert np.array_equal(x, xd)
     check_against_oracle(a, b, c, d, x, dtype=dt)
     if prec == "f32":
         legacy_accept(x, a, b, c, d)
@@ -226,6 +233,50 @@ def test_dropin_pinned_arrays_solved_in_place(cuda, prec, n):
             check_ulps(x_in.reshape(m, n), x_st.reshape(m, n), ulps=64)
         else:
             assert np.array_equal(x_in, x_st), name
+    for p, v in zip((pa, pb, pc, pd), (a, b, c, d)):
+        assert np.array_equal(p, np.ascontiguousarray(v).reshape(-1))
+    assert tg.device_status() == 0
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("n", [64, 256, 1024])
+def test_dropin_pageable_arrays_solved_in_place(cuda, n, prec):
+    """The host-pointer launchers on ordinary (pageable) numpy arrays: where
+    the device reaches pageable memory through the host's page tables
+    (tridi_dropin_pageable_in_place() = 1, as on Grace hosts) the solver works
+    on them in place; the same calls with pageable arrays staged
+    (TRIDI_TUNE_DROPIN_MAPPED = 3) and fully staged (= 2) agree -- bit for
+    bit where both paths run the same CR arithmetic -- and a..d are left
+    unchanged."""
+    from tridiagonalsolvers_gb300._lib import lib
+
+    L = lib()
+    print("pageable in place:", L.tridi_dropin_pageable_in_place())
+    dt = NP[prec]
+    m = 301
+    a, b, c, d = workloads.dominant(m, n, seed=91 + n, dtype=dt)
+    pa, pb, pc, pd = (np.ascontiguousarray(v).reshape(-1).copy() for v in (a, b, c, d))
+    launchers = [("cr", dropin.cr, ()), ("pcr", dropin.pcr, ()), ("crpcr", dropin.crpcr, (16,)),
+                 ("crNBC", dropin.crNBC, ()), ("crNBC32", dropin.crNBC32, ()),
+                 ("crpcrNBC", dropin.crpcrNBC, (16,))]
+    for name, fn, extra in launchers:
+        x_in = np.ones(m * n, dt)
+        fn(pa, pb, pc, pd, x_in, n, m, *extra)
+        check_against_oracle(a, b, c, d, x_in.reshape(m, n), dtype=dt)
+        for mode in (3, 2):
+            x_st = np.ones(m * n, dt)
+            assert L.tridi_set_tunable(11, mode) == 0
+            try:
+                fn(pa, pb, pc, pd, x_st, n, m, *extra)
+            finally:
+                L.tridi_set_tunable(11, 0)
+            check_against_oracle(a, b, c, d, x_st.reshape(m, n), dtype=dt)
+            # staged, pcr and crpcr at 1024 unknowns take the two-phase / register PCR kernels;
+            # in place, the hybrid kernel's PCR (plain loads): the same algorithm, other rounding
+            if name == "pcr" or (prec == "f32" and n == 1024 and name in ("crpcr", "crpcrNBC")):
+                check_ulps(x_in.reshape(m, n), x_st.reshape(m, n), ulps=64)
+            else:
+                assert np.array_equal(x_in, x_st), (name, mode)
     for p, v in zip((pa, pb, pc, pd), (a, b, c, d)):
         assert np.array_equal(p, np.ascontiguousarray(v).reshape(-1))
     assert tg.device_status() == 0

@@ -81,6 +81,34 @@ P* mapped_view(P* p) {
   return at.type == cudaMemoryTypeHost ? static_cast<P*>(at.devicePointer) : nullptr;
 }
 
+// Ordinary (pageable) host memory: neither pinned nor device memory.
+template <class P>
+bool pageable(P* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeUnregistered;
+}
+
+// True when device `dev` reads and writes pageable host memory coherently
+// through the host's own page tables (address translation services, as on
+// Grace hosts): then the solver can work on malloc'd arrays at their own
+// addresses.  Queried once per device (callers hold g_mu).
+bool pageable_direct(int dev) {
+  static signed char known[kMaxDev] = {};  // 0 not yet asked, 1 yes, -1 no
+  if (known[dev] == 0) {
+    int access = 0, host_tables = 0;
+    const bool ok = cudaDeviceGetAttribute(&access, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
+                    cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) ==
+                        cudaSuccess;
+    if (!ok) cudaGetLastError();
+    known[dev] = ok && access == 1 && host_tables == 1 ? 1 : -1;
+  }
+  return known[dev] == 1;
+}
+
 // Extra device scratch the algorithm needs for m systems of size n.
 template <class T>
 size_t algo_scratch(int algo, int n, int m, int param);
@@ -103,12 +131,18 @@ tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d
   // Arrays that are pinned and mapped: the solver reads a..d and writes x in
   // place over the host link.  The same bytes cross it as with staging
   // copies, but no chunk pipeline fills and drains, and no copy waits for
-  // the copy engine behind another.  The kernels then read with plain loads
-  // (g_host_mapped_io); pcrGauss, whose larger sizes take the partition and
-  // large-system solvers, always stages.
-  if (!whole_batch_scratch && algo != TRIDI_DROPIN_PCR_THOMAS && tunable(TRIDI_TUNE_DROPIN_MAPPED) != 2) {
+  // the copy engine behind another.  The same for ordinary pageable arrays
+  // where the device reaches them through the host's page tables.  The
+  // kernels then read with plain loads (g_host_mapped_io); pcrGauss, whose
+  // larger sizes take the partition and large-system solvers, always stages.
+  const int in_place = tunable(TRIDI_TUNE_DROPIN_MAPPED);
+  if (!whole_batch_scratch && algo != TRIDI_DROPIN_PCR_THOMAS && in_place != 2) {
     const T *va = mapped_view(a), *vb = mapped_view(b), *vc = mapped_view(c), *vd = mapped_view(d);
     T* vx = mapped_view(x);
+    if (!(va && vb && vc && vd && vx) && in_place != 3 && pageable_direct(dev) && pageable(a) && pageable(b) &&
+        pageable(c) && pageable(d) && pageable(x)) {
+      va = a; vb = b; vc = c; vd = d; vx = x;
+    }
     if (va && vb && vc && vd && vx) {
       e = ensure_workspace(w, 0);
       if (e != cudaSuccess) return cuda_status(e);
@@ -296,6 +330,15 @@ tridi_status tridi_dropin_solve_f32(int algo, const float* a, const float* b, co
 tridi_status tridi_dropin_solve_f64(int algo, const double* a, const double* b, const double* c, const double* d,
                                     double* x, int n, int m, int param) {
   return tridi::host_solve<double>(algo, a, b, c, d, x, n, m, param);
+}
+int tridi_dropin_pageable_in_place(void) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= tridi::kMaxDev) {
+    cudaGetLastError();
+    return 0;
+  }
+  std::lock_guard<std::mutex> lock(tridi::g_mu);
+  return tridi::pageable_direct(dev) ? 1 : 0;
 }
 }  // extern "C"
 
