@@ -282,6 +282,40 @@ def test_dropin_pageable_arrays_solved_in_place(cuda, n, prec):
     assert tg.device_status() == 0
 
 
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_dropin_pageable_every_launcher_and_size(cuda, prec):
+    """Every host-pointer launcher at every power-of-two size its kernels
+    take, on pageable arrays: the in-place path (where the device reaches
+    pageable memory) returns the staged path's status and its answer passes
+    the FP64 oracle, within a few ulp of the staged answer."""
+    from tridiagonalsolvers_gb300._lib import lib
+
+    L = lib()
+    dt = NP[prec]
+    f = L.tridi_dropin_solve_f32 if prec == "f32" else L.tridi_dropin_solve_f64
+    nmax = 4096 if prec == "f32" else 2048
+    m = 3
+    for algo, name in enumerate(["cr", "pcr", "crpcr", "crNBC", "crpcrNBC", "crNBC32"]):
+        n = 2
+        while n <= nmax:
+            a, b, c, d = (np.ascontiguousarray(v).reshape(-1) for v in workloads.dominant(m, n, seed=n, dtype=dt))
+            param = max(2, n // 4) if name in ("crpcr", "crpcrNBC") else 0
+            x_in, x_st = np.ones(m * n, dt), np.ones(m * n, dt)
+            s_in = f(algo, *(v.ctypes.data for v in (a, b, c, d, x_in)), n, m, param)
+            assert L.tridi_set_tunable(11, 3) == 0
+            try:
+                s_st = f(algo, *(v.ctypes.data for v in (a, b, c, d, x_st)), n, m, param)
+            finally:
+                L.tridi_set_tunable(11, 0)
+            assert s_in == s_st, (name, n, L.tridi_status_string(s_in), L.tridi_status_string(s_st))
+            if s_in == 0:
+                check_against_oracle(a.reshape(m, n), b.reshape(m, n), c.reshape(m, n), d.reshape(m, n),
+                                     x_in.reshape(m, n), dtype=dt)
+                check_ulps(x_in.reshape(m, n), x_st.reshape(m, n), ulps=64)
+            n *= 2
+    assert tg.device_status() == 0
+
+
 @pytest.mark.parametrize("n", [2, 8, 32, 64, 512, 2048, 4096])
 def test_dropin_pinned_cr_sizes(cuda, n):
     """cr() on pinned, mapped arrays across the system sizes (warp and block

@@ -50,6 +50,7 @@ for _prec in ("f32", "f64"):
     _SIGS[f"tridi_solve_large_{_prec}"] = (c_int, [_P, _P, _P, _P, _P, ctypes.c_long, ctypes.c_long, c_int, _P,
                                                    c_size_t, _P])
 _SIGS["tridi_dropin_release"] = (c_int, [])
+_SIGS["tridi_dropin_pageable_in_place"] = (c_int, [])
 _SIGS["tridi_write_result_file_f32"] = (c_int, [_P, c_int, c_int, c_char_p])
 _SIGS["tridi_write_result_file_f64"] = (c_int, [_P, c_int, c_int, c_char_p])
 _SIGS["tridi_large_workspace_bytes"] = (c_size_t, [ctypes.c_long, ctypes.c_long, c_int])
