@@ -57,6 +57,7 @@ struct XNext;
 template <>
 struct XNext<false> {
   using V = double;
+  static constexpr int kMinBlocks = 3;  // blocks an SM of the interleaved residual kernel (80 registers)
   __device__ __forceinline__ static V get(const RefineParams& p, long k) {
     return p.first ? (double)p.e[k] : p.xin[k] + (double)p.e[k];
   }
@@ -87,6 +88,9 @@ struct XNext<false> {
 template <int MODE>
 struct XDF {
   using V = float2;
+  // blocks an SM of the interleaved residual kernel: 64 registers (no spill) in
+  // the first sweep's form, 80 in the others (at 64 they spill)
+  static constexpr int kMinBlocks = MODE == 0 ? 4 : 3;
   __device__ __forceinline__ static V get(const RefineParams& p, long k) {
     if constexpr (MODE == 0) return make_float2(p.e[k], 0.f);
     else if constexpr (MODE == 1) return df_add(make_float2(p.x1f[k], 0.f), p.e[k]);
@@ -188,12 +192,11 @@ __global__ void __launch_bounds__(256) refine_contig_kernel(RefineParams p) {
 // rows go in batches of kBatch whose loads are all issued before any of their
 // residuals (the stores of r and x alias nothing the loads read, but the
 // compiler cannot know that), so a warp keeps kBatch rows of loads in flight.
-// Two rows at four blocks an SM measured best (1024 x 65536, one refinement:
-// double-float 1.84 ms, FP64 3.50 ms, against 1.91 / 4.09 ms for one row at a
-// time with x of every neighbour reloaded; four rows at two blocks an SM
-// 2.07 / 3.79 ms).
+// Two rows measured best (1024 x 65536, one refinement: double-float 1.84 ms,
+// FP64 3.50 ms, against 1.91 / 4.09 ms for one row at a time with x of every
+// neighbour reloaded; four rows at two blocks an SM 2.07 / 3.79 ms).
 template <class X>
-__global__ void __launch_bounds__(256, 4) refine_inter_kernel(RefineParams p) {
+__global__ void __launch_bounds__(256, X::kMinBlocks) refine_inter_kernel(RefineParams p) {
   constexpr int kBatch = 2;
   using V = typename X::V;
   const long groups = (p.m + 31) / 32;
