@@ -97,23 +97,29 @@ __global__ void __launch_bounds__(kWarps * 32, 3)
     if (lane == 0 && tile + step < tiles) issue(tile + step);
     if (lane == 0) v[0][0] = 0.0f;          // a[0] is not part of the system
     if (lane == 31) v[2][kR - 1] = 0.0f;    // nor is c[n-1]
-    // ---- CR level: odd rows 2j+1 against their even neighbours ----
+    // ---- CR level: odd rows 2j+1 against their even neighbours, which are
+    //      normalised once (one reciprocal per even row; the back
+    //      substitution reuses them) ----
     // (lane 31's last odd row has c = 0, so the shuffled-in neighbour, its
     // own first row, contributes nothing)
-    const float ra = __shfl_down_sync(kFull, v[0][0], 1), rb = __shfl_down_sync(kFull, v[1][0], 1);
-    const float rc = __shfl_down_sync(kFull, v[2][0], 1), rd = __shfl_down_sync(kFull, v[3][0], 1);
+    NR e[kRR];  // even row 2j / its diagonal
+#pragma unroll
+    for (int j = 0; j < kRR; ++j) {
+      const float ib = rcp_approx(v[1][2 * j]);
+      e[j] = NR{v[0][2 * j] * ib, v[2][2 * j] * ib, v[3][2 * j] * ib};
+    }
+    const NR eR = shfl_down_nr(e[0], 32);  // the next lane's row 0
     NR2 P[kRR / 2];
 #pragma unroll
     for (int j = 0; j < kRR; ++j) {
       const int q = 2 * j + 1;
-      const float aR = q + 1 < kR ? v[0][q + 1] : ra, bR = q + 1 < kR ? v[1][q + 1] : rb;
-      const float cR = q + 1 < kR ? v[2][q + 1] : rc, dR = q + 1 < kR ? v[3][q + 1] : rd;
-      const float k1 = tdiv(v[0][q], v[1][q - 1]);
-      const float k2 = tdiv(v[2][q], bR);
-      const float an = -v[0][q - 1] * k1;
-      const float bn = v[1][q] - v[2][q - 1] * k1 - aR * k2;
-      const float cn = -cR * k2;
-      const float dn = v[3][q] - v[3][q - 1] * k1 - dR * k2;
+      const NR& L = e[j];
+      const NR& Rn = j + 1 < kRR ? e[j + 1] : eR;
+      const float aq = v[0][q], cq = v[2][q];
+      const float an = -aq * L.a;
+      const float bn = v[1][q] - aq * L.c - cq * Rn.a;
+      const float cn = -cq * Rn.c;
+      const float dn = v[3][q] - aq * L.d - cq * Rn.d;
       const float ib = rcp_approx(bn);
       const NR r{an * ib, cn * ib, dn * ib};
       if (j & 1) {
@@ -163,7 +169,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3)
     for (int j = 0; j < kRR; ++j) {
       const float xodd = sw[xr_index(kRR * lane + j)];
       const int q = 2 * j;
-      xo[q] = (v[3][q] - v[0][q] * xprev - v[2][q] * xodd) * rcp_approx(v[1][q]);
+      xo[q] = e[j].d - e[j].a * xprev - e[j].c * xodd;
       xo[q + 1] = xodd;
       xprev = xodd;
     }
@@ -212,6 +218,51 @@ __device__ __forceinline__ void cr_back(const float (&a)[K], const float (&b)[K]
 #pragma unroll
   for (int j = 0; j < K / 2; ++j) {
     x[2 * j] = (d[2 * j] - a[2 * j] * xprev - c[2 * j] * xo[j]) * rcp_approx(b[2 * j]);
+    x[2 * j + 1] = xo[j];
+    xprev = xo[j];
+  }
+}
+
+// The same level with the even rows normalised first, (ea, ec, ed) = (a, c, d)
+// / b of row 2j: one reciprocal per even row instead of two per odd row, and
+// the back substitution (cr_back_norm) needs none.  The eliminations then
+// take the form me - a_q L' - c_q R' with normalised neighbours, which rounds
+// differently from CR's own divisions (used where crpcr switches above 2).
+template <int K>
+__device__ __forceinline__ void cr_level_norm(const float (&a)[K], const float (&b)[K], const float (&c)[K],
+                                              const float (&d)[K], float (&ea)[K / 2], float (&ec)[K / 2],
+                                              float (&ed)[K / 2], float (&na)[K / 2], float (&nb)[K / 2],
+                                              float (&nc)[K / 2], float (&nd)[K / 2]) {
+#pragma unroll
+  for (int j = 0; j < K / 2; ++j) {
+    const float ib = rcp_approx(b[2 * j]);
+    ea[j] = a[2 * j] * ib;
+    ec[j] = c[2 * j] * ib;
+    ed[j] = d[2 * j] * ib;
+  }
+  const float ra = __shfl_down_sync(kFull, ea[0], 1), rc = __shfl_down_sync(kFull, ec[0], 1);
+  const float rd = __shfl_down_sync(kFull, ed[0], 1);
+#pragma unroll
+  for (int j = 0; j < K / 2; ++j) {
+    const int q = 2 * j + 1;
+    const float Ra = j + 1 < K / 2 ? ea[j + 1] : ra, Rc = j + 1 < K / 2 ? ec[j + 1] : rc;
+    const float Rd = j + 1 < K / 2 ? ed[j + 1] : rd;
+    na[j] = -a[q] * ea[j];
+    nb[j] = b[q] - a[q] * ec[j] - c[q] * Ra;
+    nc[j] = -c[q] * Rc;
+    nd[j] = d[q] - a[q] * ed[j] - c[q] * Rd;
+  }
+}
+
+template <int K>
+__device__ __forceinline__ void cr_back_norm(const float (&ea)[K / 2], const float (&ec)[K / 2],
+                                             const float (&ed)[K / 2], const float (&xo)[K / 2], float (&x)[K],
+                                             int lane) {
+  float xprev = __shfl_up_sync(kFull, xo[K / 2 - 1], 1);
+  if (lane == 0) xprev = 0.0f;
+#pragma unroll
+  for (int j = 0; j < K / 2; ++j) {
+    x[2 * j] = ed[j] - ea[j] * xprev - ec[j] * xo[j];
     x[2 * j + 1] = xo[j];
     xprev = xo[j];
   }
@@ -318,16 +369,26 @@ __device__ __forceinline__ float cr_cross(float a, float b, float c, float d, in
 }
 
 // LEV CR levels down from the lane's K rows (the levels past K = 1 between
-// lanes), the PCR, and the back substitutions up again.
-template <int K, int LEV>
+// lanes), the PCR, and the back substitutions up again.  NORM: the in-lane
+// levels on normalised even rows (cr_level_norm); else CR's own arithmetic.
+template <int K, int LEV, bool NORM>
 __device__ __forceinline__ void cr_solve(const float (&a)[K], const float (&b)[K], const float (&c)[K],
                                          const float (&d)[K], float (&x)[K], int lane) {
   float na[K / 2], nb[K / 2], nc[K / 2], nd[K / 2], xo[K / 2];
-  cr_level<K>(a, b, c, d, na, nb, nc, nd);
-  if constexpr (LEV == 1) pcr_lanes<K / 2, 1>(na, nb, nc, nd, xo, lane);
-  else if constexpr (K == 2) xo[0] = cr_cross<LEV - 1>(na[0], nb[0], nc[0], nd[0], lane);
-  else cr_solve<K / 2, LEV - 1>(na, nb, nc, nd, xo, lane);
-  cr_back<K>(a, b, c, d, xo, x, lane);
+  if constexpr (NORM) {
+    float ea[K / 2], ec[K / 2], ed[K / 2];
+    cr_level_norm<K>(a, b, c, d, ea, ec, ed, na, nb, nc, nd);
+    if constexpr (LEV == 1) pcr_lanes<K / 2, 1>(na, nb, nc, nd, xo, lane);
+    else if constexpr (K == 2) xo[0] = cr_cross<LEV - 1>(na[0], nb[0], nc[0], nd[0], lane);
+    else cr_solve<K / 2, LEV - 1, NORM>(na, nb, nc, nd, xo, lane);
+    cr_back_norm<K>(ea, ec, ed, xo, x, lane);
+  } else {
+    cr_level<K>(a, b, c, d, na, nb, nc, nd);
+    if constexpr (LEV == 1) pcr_lanes<K / 2, 1>(na, nb, nc, nd, xo, lane);
+    else if constexpr (K == 2) xo[0] = cr_cross<LEV - 1>(na[0], nb[0], nc[0], nd[0], lane);
+    else cr_solve<K / 2, LEV - 1, NORM>(na, nb, nc, nd, xo, lane);
+    cr_back<K>(a, b, c, d, xo, x, lane);
+  }
 }
 
 constexpr size_t kSmemLanes = 128 + 1024 + (size_t)kWarps * 4 * kTF * 4;
@@ -387,7 +448,8 @@ __global__ void __launch_bounds__(kWarps * 32, 4)
     if (lane == 0) v[0][0] = 0.0f;
     if (lane == 31) v[2][kR - 1] = 0.0f;
     float x[kR];
-    cr_solve<kR, LEV>(v[0], v[1], v[2], v[3], x, lane);
+    // rest 2 is cr: CR's own arithmetic, bit for bit that of the other CR kernels
+    cr_solve<kR, LEV, (LEV < 9)>(v[0], v[1], v[2], v[3], x, lane);
     float4* dst = reinterpret_cast<float4*>(gx + tile * kN + kR * lane);
 #pragma unroll
     for (int q = 0; q < kR / 4; ++q) dst[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
