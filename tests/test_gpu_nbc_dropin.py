@@ -229,7 +229,9 @@ def test_dropin_pinned_arrays_solved_in_place(cuda, prec, n):
             L.tridi_set_tunable(11, 0)
         check_against_oracle(a, b, c, d, x_in.reshape(m, n), dtype=dt)
         check_against_oracle(a, b, c, d, x_st.reshape(m, n), dtype=dt)
-        if name == "pcr":  # staged: the two-phase PCR kernel; in place: the hybrid kernel's PCR
+        # staged, pcr and crpcr at 1024 unknowns take the two-phase / register PCR kernels;
+        # in place, the hybrid kernel's (plain loads): the same algorithm, other rounding
+        if name == "pcr" or (prec == "f32" and n == 1024 and name in ("crpcr", "crpcrNBC")):
             check_ulps(x_in.reshape(m, n), x_st.reshape(m, n), ulps=64)
         else:
             assert np.array_equal(x_in, x_st), name

@@ -69,27 +69,20 @@ cudaError_t ensure_workspace(Workspace& w, size_t bytes) {
 
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
-// The device's address of host memory that is pinned and mapped into its
-// address space (cudaHostAlloc, cudaHostRegister with mapping), else null.
+// What a host pointer is: `view` = the device's address of host memory that
+// is pinned and mapped into its address space (cudaHostAlloc,
+// cudaHostRegister with mapping), else null; `pageable` = ordinary host
+// memory, neither pinned nor device memory.  One query a pointer.
 template <class P>
-P* mapped_view(P* p) {
+P* host_view(P* p, bool& pageable) {
   cudaPointerAttributes at{};
+  pageable = false;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();  // unregistered memory on older drivers: not an error of the call
     return nullptr;
   }
+  pageable = at.type == cudaMemoryTypeUnregistered;
   return at.type == cudaMemoryTypeHost ? static_cast<P*>(at.devicePointer) : nullptr;
-}
-
-// Ordinary (pageable) host memory: neither pinned nor device memory.
-template <class P>
-bool pageable(P* p) {
-  cudaPointerAttributes at{};
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeUnregistered;
 }
 
 // True when device `dev` reads and writes pageable host memory coherently
@@ -137,10 +130,10 @@ tridi_status host_solve(int algo, const T* a, const T* b, const T* c, const T* d
   // larger sizes take the partition and large-system solvers, always stages.
   const int in_place = tunable(TRIDI_TUNE_DROPIN_MAPPED);
   if (!whole_batch_scratch && algo != TRIDI_DROPIN_PCR_THOMAS && in_place != 2) {
-    const T *va = mapped_view(a), *vb = mapped_view(b), *vc = mapped_view(c), *vd = mapped_view(d);
-    T* vx = mapped_view(x);
-    if (!(va && vb && vc && vd && vx) && in_place != 3 && pageable_direct(dev) && pageable(a) && pageable(b) &&
-        pageable(c) && pageable(d) && pageable(x)) {
+    bool pa, pb, pc, pd, px;
+    const T *va = host_view(a, pa), *vb = host_view(b, pb), *vc = host_view(c, pc), *vd = host_view(d, pd);
+    T* vx = host_view(x, px);
+    if (!(va && vb && vc && vd && vx) && in_place != 3 && pa && pb && pc && pd && px && pageable_direct(dev)) {
       va = a; vb = b; vc = c; vd = d; vx = x;
     }
     if (va && vb && vc && vd && vx) {
