@@ -58,6 +58,7 @@ template <>
 struct XNext<false> {
   using V = double;
   static constexpr int kMinBlocks = 3;  // blocks an SM of the interleaved residual kernel (80 registers)
+  static constexpr int kBatch = 2;      // rows a warp loads ahead there
   __device__ __forceinline__ static V get(const RefineParams& p, long k) {
     return p.first ? (double)p.e[k] : p.xin[k] + (double)p.e[k];
   }
@@ -88,9 +89,13 @@ struct XNext<false> {
 template <int MODE>
 struct XDF {
   using V = float2;
-  // blocks an SM of the interleaved residual kernel: 64 registers (no spill) in
-  // the first sweep's form, 80 in the others (at 64 they spill)
-  static constexpr int kMinBlocks = MODE == 0 ? 4 : 3;
+  // blocks an SM and rows a warp loads ahead in the interleaved residual
+  // kernel, no form spilling: the first sweep's 2 rows at 64 registers, the
+  // second sweep's (which also assembles x in FP64) 1 row at 56 (2 rows at 64
+  // spilled, at 80 registers and 3 blocks it ran 5 % slower), later sweeps 2
+  // rows at 80
+  static constexpr int kMinBlocks = MODE == 2 ? 3 : 4;
+  static constexpr int kBatch = MODE == 1 ? 1 : 2;
   __device__ __forceinline__ static V get(const RefineParams& p, long k) {
     if constexpr (MODE == 0) return make_float2(p.e[k], 0.f);
     else if constexpr (MODE == 1) return df_add(make_float2(p.x1f[k], 0.f), p.e[k]);
@@ -192,12 +197,13 @@ __global__ void __launch_bounds__(256) refine_contig_kernel(RefineParams p) {
 // rows go in batches of kBatch whose loads are all issued before any of their
 // residuals (the stores of r and x alias nothing the loads read, but the
 // compiler cannot know that), so a warp keeps kBatch rows of loads in flight.
-// Two rows measured best (1024 x 65536, one refinement: double-float 1.84 ms,
-// FP64 3.50 ms, against 1.91 / 4.09 ms for one row at a time with x of every
-// neighbour reloaded; four rows at two blocks an SM 2.07 / 3.79 ms).
+// Measured on 1024 x 65536, one refinement: double-float 1.76 ms and FP64
+// 3.50 ms with the per-form settings below, against 1.91 / 4.09 ms for one row
+// at a time with x of every neighbour reloaded (four rows at two blocks an SM:
+// 2.07 / 3.79 ms).
 template <class X>
 __global__ void __launch_bounds__(256, X::kMinBlocks) refine_inter_kernel(RefineParams p) {
-  constexpr int kBatch = 2;
+  constexpr int kBatch = X::kBatch;
   using V = typename X::V;
   const long groups = (p.m + 31) / 32;
   const long g = blockIdx.x % groups, q = blockIdx.x / groups;
