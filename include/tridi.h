@@ -94,6 +94,9 @@ tridi_status tridi_device_status(unsigned *bits, int reset);
                                      through the host's page tables, are read and written in place by
                                      the solver (no staging copies), 2 = always staged through device
                                      memory, 3 = in place for pinned arrays only */
+#define TRIDI_TUNE_RAGGED_ORDER 12  /* plain ragged plans created afterwards: 0/1 = team items in rounds interleaved
+                                     from the largest and the smallest, 2 = largest first throughout (refinement
+                                     plans are always largest first) */
 tridi_status tridi_set_tunable(int key, int value);
 int tridi_get_tunable(int key);
 

@@ -1150,6 +1150,32 @@ tridi_status plan_create(const long* offsets, int num_systems, bool refine, void
     }
     team_items.push_back(it);
   }
+  // Plain solves: CTA b takes the list's items b, b + G, b + 2G, ... (G = the
+  // launch's CTAs), so every run of G consecutive items gives each CTA one.
+  // The team items go in such rounds of the size order interleaved from both
+  // ends -- largest round, smallest, second largest, ... -- so each CTA's
+  // teams alternate large and small items and its ring holds fewer large ones
+  // at a time (100000-system batch: 0.679 -> 0.636 ms).  A last, partial round
+  // stays last, keeping the rounds before it aligned with the CTAs.  The
+  // refinement, bound by its arithmetic rather than by the ring, keeps the
+  // largest-first order (interleaved: 1.81 -> 1.93 ms).
+  const DeviceInfo* dev = refine ? nullptr : current_device();
+  const long nall = (long)(cta_items.size() + team_items.size());
+  const long G = dev ? std::min<long>(dev->sm_count, nall) : 0;
+  if (G > 0 && (long)team_items.size() >= 2 * G && tunable(TRIDI_TUNE_RAGGED_ORDER) != 2) {
+    const long R = (long)team_items.size() / G;  // full rounds
+    std::vector<RagItem> mixed;
+    mixed.reserve(team_items.size());
+    const auto round = [&](long r) {
+      mixed.insert(mixed.end(), team_items.begin() + r * G, team_items.begin() + (r + 1) * G);
+    };
+    for (long lo = 0, hi = R; lo < hi;) {
+      round(lo++);
+      if (lo < hi) round(--hi);
+    }
+    mixed.insert(mixed.end(), team_items.begin() + R * G, team_items.end());
+    team_items.swap(mixed);
+  }
   for (const RagItem& it : cta_items) {
     if (it.kind == kBig) plan->has_big = true;
     if (it.kind == kSingle) plan->max_single_rows = std::max(plan->max_single_rows, it.rows);

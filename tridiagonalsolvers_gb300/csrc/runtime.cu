@@ -11,7 +11,7 @@ constexpr int kMaxDevices = 64;
 DeviceInfo g_dev[kMaxDevices];
 std::mutex g_mu;
 thread_local int t_last_cuda_error = 0;
-constexpr int kTunables = 12;
+constexpr int kTunables = 13;
 int g_tunable[kTunables] = {};
 }  // namespace
 
