@@ -65,20 +65,22 @@ def test_crpcr_switch_level_sweep(cuda, n, prec):
         rest *= 2
 
 
-@pytest.mark.parametrize("rest", [2, 4, 8, 16, 32, 64, 128, 256, 512])
-def test_crpcr_1024_register_kernels(cuda, rest):
-    """The register CR-PCR kernels for 1024 unknowns (FP32, every switch
-    level; rest 2 is cr), on one system, a few, and more systems than one
-    wave of warps holds (so warps loop over tiles): against the FP64 oracle,
-    and against the shared-memory kernel (TRIDI_TUNE_PCR_KERNEL = 2): bit for
-    bit at rest 2 (the same CR arithmetic), within a few ulp above (the
-    register kernels' PCR works on normalised rows)."""
+@pytest.mark.parametrize("n,rest", [(1024, r) for r in (2, 4, 8, 16, 32, 64, 128, 256, 512)]
+                         + [(512, r) for r in (2, 4, 16, 64, 256)])
+def test_crpcr_register_kernels(cuda, n, rest):
+    """The register CR-PCR kernels (FP32, 1024 unknowns: every switch level;
+    512 unknowns: batches of 4096 systems and more; rest 2 is cr), on batches
+    of one system, a few and more than one wave of warps holds (so warps loop
+    over tiles): against the FP64 oracle, and against the shared-memory kernel
+    (TRIDI_TUNE_PCR_KERNEL = 2): bit for bit at rest 2 (the same CR
+    arithmetic), within a few ulp above (the register kernels' CR levels and
+    PCR work on normalised rows)."""
     from tridiagonalsolvers_gb300._lib import lib
 
     L = lib()
-    n = 1024
-    for m in (1, 5, 2 * 152 * 4 * 2 + 3):
-        a, b, c, d = workloads.dominant(m, n, seed=13 * m + rest)
+    ms = (1, 5, 2 * 152 * 4 * 2 + 3) if n == 1024 else (4096, 2 * 152 * 8 * 2 + 5)
+    for m in ms:
+        a, b, c, d = workloads.dominant(m, n, seed=13 * m + rest + n)
         t = _dev(cuda, a, b, c, d)
         x = tg.crpcr(*t, rest).cpu().numpy()
         check_against_oracle(a, b, c, d, x)

@@ -395,22 +395,26 @@ __device__ __forceinline__ void cr_solve(const float (&a)[K], const float (&b)[K
   }
 }
 
-constexpr size_t kSmemLanes = 128 + 1024 + (size_t)kWarps * 4 * kTF * 4;
+// Shared memory of a lanes-kernel CTA for n unknowns: barriers, then the two
+// warps' TMA buffers (1024-byte aligned for the 128-byte swizzle).
+constexpr size_t lanes_smem(int n) { return 128 + 1024 + (size_t)kWarps * 4 * n * 4; }
 
-// CR-PCR with the switch at 1024 / 2^LEV for 1024 unknowns, in registers and
-// shuffles (the file header gives the scheme).  Four CTAs of two warps an SM
-// (at most 255 registers: none spill); three or five to six measured the same
-// or slower.
-template <int LEV>
-__global__ void __launch_bounds__(kWarps * 32, 4)
+// CR-PCR with the switch at N / 2^LEV for N = 512 or 1024 unknowns (R = N / 32
+// rows a lane), in registers and shuffles (the file header gives the scheme).
+// At 1024 unknowns four CTAs of two warps an SM (at most 255 registers: none
+// spill; three or five to six measured the same or slower), at 512 eight (the
+// same bytes of tiles in flight an SM).
+template <int N, int LEV>
+__global__ void __launch_bounds__(kWarps * 32, N == 512 ? 8 : 4)
     crpcr_lanes_kernel(HybridParams p, const __grid_constant__ CUtensorMap ma, const __grid_constant__ CUtensorMap mb,
                        const __grid_constant__ CUtensorMap mc, const __grid_constant__ CUtensorMap md) {
+  constexpr int R = N / 32, TF = N;
   extern __shared__ __align__(128) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem) + warp;
   const uint32_t base = smem_addr(smem);
   const uint32_t ring = (base + 128 + 1023) & ~1023u;
-  float* buf = reinterpret_cast<float*>(smem + (ring - base)) + (size_t)warp * 4 * kTF;
+  float* buf = reinterpret_cast<float*>(smem + (ring - base)) + (size_t)warp * 4 * TF;
   float* gx = static_cast<float*>(p.x);
   const long tiles = p.m;
   const long first = (long)blockIdx.x * kWarps + warp;
@@ -421,53 +425,54 @@ __global__ void __launch_bounds__(kWarps * 32, 4)
   }
   __syncwarp();
   const auto issue = [&](long tile) {
-    const int row = (int)(tile * (kTF / 32));
-    mbar_arrive_expect_tx(bar, 4 * kTF * sizeof(float));
-    tma_load_2d(buf + 0 * kTF, &ma, 0, row, bar);
-    tma_load_2d(buf + 1 * kTF, &mb, 0, row, bar);
-    tma_load_2d(buf + 2 * kTF, &mc, 0, row, bar);
-    tma_load_2d(buf + 3 * kTF, &md, 0, row, bar);
+    const int row = (int)(tile * (TF / 32));
+    mbar_arrive_expect_tx(bar, 4 * TF * sizeof(float));
+    tma_load_2d(buf + 0 * TF, &ma, 0, row, bar);
+    tma_load_2d(buf + 1 * TF, &mb, 0, row, bar);
+    tma_load_2d(buf + 2 * TF, &mc, 0, row, bar);
+    tma_load_2d(buf + 3 * TF, &md, 0, row, bar);
   };
   if (lane == 0 && first < tiles) issue(first);
-  int chunk[kR / 4];
+  int chunk[R / 4];
 #pragma unroll
-  for (int q = 0; q < kR / 4; ++q) {
-    const int c = lane * (kR / 4) + q, row = c >> 3;
+  for (int q = 0; q < R / 4; ++q) {
+    const int c = lane * (R / 4) + q, row = c >> 3;
     chunk[q] = row * 32 + (((c & 7) ^ (row & 7)) << 2);
   }
   int k = 0;
   for (long tile = first; tile < tiles; tile += step, ++k) {
     if (!mbar_wait(bar, k & 1, p.status)) break;
-    float v[4][kR];
+    float v[4][R];
 #pragma unroll
     for (int arr = 0; arr < 4; ++arr)
 #pragma unroll
-      for (int q = 0; q < kR / 4; ++q) {
-        const float4 f = *reinterpret_cast<const float4*>(buf + arr * kTF + chunk[q]);
+      for (int q = 0; q < R / 4; ++q) {
+        const float4 f = *reinterpret_cast<const float4*>(buf + arr * TF + chunk[q]);
         v[arr][4 * q] = f.x; v[arr][4 * q + 1] = f.y; v[arr][4 * q + 2] = f.z; v[arr][4 * q + 3] = f.w;
       }
     fence_proxy_async_smem();
     __syncwarp();
     if (lane == 0 && tile + step < tiles) issue(tile + step);
     if (lane == 0) v[0][0] = 0.0f;
-    if (lane == 31) v[2][kR - 1] = 0.0f;
-    float x[kR];
+    if (lane == 31) v[2][R - 1] = 0.0f;
+    float x[R];
     // rest 2 is cr: CR's own arithmetic, bit for bit that of the other CR kernels
-    cr_solve<kR, LEV, (LEV < 9)>(v[0], v[1], v[2], v[3], x, lane);
-    float4* dst = reinterpret_cast<float4*>(gx + tile * kN + kR * lane);
+    cr_solve<R, LEV, ((N >> LEV) > 2)>(v[0], v[1], v[2], v[3], x, lane);
+    float4* dst = reinterpret_cast<float4*>(gx + tile * N + R * lane);
 #pragma unroll
-    for (int q = 0; q < kR / 4; ++q) dst[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+    for (int q = 0; q < R / 4; ++q) dst[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
   }
 }
 
 using TileKernel = void (*)(HybridParams, CUtensorMap, CUtensorMap, CUtensorMap, CUtensorMap);
 
-// One warp a system, as many CTAs of two warps as fit on every SM up to four
-// (the warps then loop over the batch).  Five or six CTAs an SM, where the
-// registers allow it, measured 5 % slower: more warps contend for the
-// shared-memory pipe without hiding more DRAM latency.
-tridi_status launch_tiles(TileKernel kern, size_t smem, const HybridParams& p, const CUtensorMap* tm,
-                          const DeviceInfo* dev, cudaStream_t stream) {
+// One warp a system, as many CTAs of two warps as fit on every SM up to
+// max_per_sm (the warps then loop over the batch).  At 1024 unknowns five or
+// six CTAs an SM, where the registers allow it, measured 5 % slower than four:
+// more warps contend for the shared-memory pipe without hiding more DRAM
+// latency.
+tridi_status launch_tiles(TileKernel kern, size_t smem, int max_per_sm, const HybridParams& p,
+                          const CUtensorMap* tm, const DeviceInfo* dev, cudaStream_t stream) {
   if (smem > (size_t)dev->max_smem_optin) return TRIDI_ERROR_UNSUPPORTED_SIZE;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e);
@@ -475,52 +480,72 @@ tridi_status launch_tiles(TileKernel kern, size_t smem, const HybridParams& p, c
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
   if (e != cudaSuccess) return cuda_status(e);
   if (per_sm < 1) per_sm = 1;
-  if (per_sm > 4) per_sm = 4;
+  if (per_sm > max_per_sm) per_sm = max_per_sm;
   long grid = (long)per_sm * dev->sm_count;
   if (grid * kWarps > p.m) grid = (p.m + kWarps - 1) / kWarps;
   kern<<<(unsigned)grid, kWarps * 32, smem, stream>>>(p, tm[0], tm[1], tm[2], tm[3]);
   return cuda_status(cudaGetLastError());
 }
 
+template <int N>
+tridi_status launch_lanes(int stride, const HybridParams& p, const CUtensorMap* tm, const DeviceInfo* dev,
+                          cudaStream_t stream) {
+  constexpr int M = N == 512 ? 8 : 4;
+  constexpr size_t S = lanes_smem(N);
+  switch (stride) {
+    case 2: if constexpr (N == 512) return launch_tiles(crpcr_lanes_kernel<N, 1>, S, M, p, tm, dev, stream);
+            break;
+    case 4: return launch_tiles(crpcr_lanes_kernel<N, 2>, S, M, p, tm, dev, stream);
+    case 8: return launch_tiles(crpcr_lanes_kernel<N, 3>, S, M, p, tm, dev, stream);
+    case 16: return launch_tiles(crpcr_lanes_kernel<N, 4>, S, M, p, tm, dev, stream);
+    case 32: return launch_tiles(crpcr_lanes_kernel<N, 5>, S, M, p, tm, dev, stream);
+    case 64: return launch_tiles(crpcr_lanes_kernel<N, 6>, S, M, p, tm, dev, stream);
+    case 128: return launch_tiles(crpcr_lanes_kernel<N, 7>, S, M, p, tm, dev, stream);
+    case 256: return launch_tiles(crpcr_lanes_kernel<N, 8>, S, M, p, tm, dev, stream);
+    case 512: if constexpr (N == 1024) return launch_tiles(crpcr_lanes_kernel<N, 9>, S, M, p, tm, dev, stream);
+              break;
+    default: break;
+  }
+  return TRIDI_ERROR_UNSUPPORTED_SIZE;
+}
+
 }  // namespace
 
 // True when a register kernel takes this FP32 call: cr, or crpcr at any
-// switch level (stride = n / rest = 2 .. 512), at n = 1024, 16-byte aligned
-// a..d and x, the batch within the tensor maps' 32-bit row count.
-bool crpcr1024_applies(const void* a, const void* b, const void* c, const void* d, const void* x, int n, long m,
-                       int stride) {
-  return n == kN && stride >= 2 && stride <= 512 && is_pow2(stride) && aligned16(a) && aligned16(b) &&
-         aligned16(c) && aligned16(d) && aligned16(x) && m * n / 32 < (1L << 31) &&
+// switch level (stride = n / rest = 2 .. n/2), at n = 1024, or at n = 512 from
+// 4096 systems up (on a small batch one warp a system leaves the GPU short of
+// threads: 512 x 512 cr 6.1 us against 4.7 us for the block kernel, which
+// gives a system two warps; 32768 x 512 cr 54.6 against 58.0 us, crpcr rest
+// 256 55.9 against 117.2 us), 16-byte aligned a..d and x, the batch within
+// the tensor maps' 32-bit row count.
+bool crpcr_regs_applies(const void* a, const void* b, const void* c, const void* d, const void* x, int n, long m,
+                        int stride) {
+  return (n == 1024 || (n == 512 && m >= 4096)) && stride >= 2 && stride <= n / 2 && is_pow2(stride) &&
+         aligned16(a) &&
+         aligned16(b) && aligned16(c) && aligned16(d) && aligned16(x) && m * n / 32 < (1L << 31) &&
          tunable(TRIDI_TUNE_PCR_KERNEL) != 2 && !g_host_mapped_io;
 }
 
-tridi_status crpcr1024_solve(const float* a, const float* b, const float* c, const float* d, float* x, int m,
-                             int stride, cudaStream_t stream) {
+tridi_status crpcr_regs_solve(const float* a, const float* b, const float* c, const float* d, float* x, int n,
+                              int m, int stride, cudaStream_t stream) {
   const DeviceInfo* dev = current_device();
   if (!dev) return TRIDI_ERROR_CUDA;
   HybridParams p{};
   p.a = a; p.b = b; p.c = c; p.d = d; p.x = x;
-  p.n = kN; p.m = m; p.stride = stride;
+  p.n = n; p.m = m; p.stride = stride;
   p.status = dev->status;
-  const uint64_t rows = (uint64_t)m * kN / 32;
+  const uint64_t rows = (uint64_t)m * n / 32;
+  const uint32_t box = (uint32_t)(n / 32);  // a system: n / 32 rows of 32 values
   CUtensorMap tma, tmb, tmc, tmd;
-  if (!make_tensor_map_2d(&tma, a, 32, rows, 128, 32, kR, true) ||
-      !make_tensor_map_2d(&tmb, b, 32, rows, 128, 32, kR, true) ||
-      !make_tensor_map_2d(&tmc, c, 32, rows, 128, 32, kR, true) ||
-      !make_tensor_map_2d(&tmd, d, 32, rows, 128, 32, kR, true))
+  if (!make_tensor_map_2d(&tma, a, 32, rows, 128, 32, box, true) ||
+      !make_tensor_map_2d(&tmb, b, 32, rows, 128, 32, box, true) ||
+      !make_tensor_map_2d(&tmc, c, 32, rows, 128, 32, box, true) ||
+      !make_tensor_map_2d(&tmd, d, 32, rows, 128, 32, box, true))
     return cuda_status(cudaErrorInvalidValue);
   const CUtensorMap tm[4] = {tma, tmb, tmc, tmd};
-  switch (stride) {
-    case 2: return launch_tiles(crpcr512_kernel, kSmem, p, tm, dev, stream);
-    case 4: return launch_tiles(crpcr_lanes_kernel<2>, kSmemLanes, p, tm, dev, stream);
-    case 8: return launch_tiles(crpcr_lanes_kernel<3>, kSmemLanes, p, tm, dev, stream);
-    case 16: return launch_tiles(crpcr_lanes_kernel<4>, kSmemLanes, p, tm, dev, stream);
-    case 32: return launch_tiles(crpcr_lanes_kernel<5>, kSmemLanes, p, tm, dev, stream);
-    case 64: return launch_tiles(crpcr_lanes_kernel<6>, kSmemLanes, p, tm, dev, stream);
-    case 128: return launch_tiles(crpcr_lanes_kernel<7>, kSmemLanes, p, tm, dev, stream);
-    case 256: return launch_tiles(crpcr_lanes_kernel<8>, kSmemLanes, p, tm, dev, stream);
-    default: return launch_tiles(crpcr_lanes_kernel<9>, kSmemLanes, p, tm, dev, stream);
-  }
+  if (n == 512) return launch_lanes<512>(stride, p, tm, dev, stream);
+  if (stride == 2) return launch_tiles(crpcr512_kernel, kSmem, 4, p, tm, dev, stream);
+  return launch_lanes<1024>(stride, p, tm, dev, stream);
 }
 
 }  // namespace tridi

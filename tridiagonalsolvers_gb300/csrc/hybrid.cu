@@ -181,7 +181,7 @@ tridi_status solve_hybrid(const T* a, const T* b, const T* c, const T* d, T* x, 
   cudaStream_t s = as_stream(stream);
   cudaError_t e = cudaErrorInvalidValue;
   if constexpr (sizeof(T) == 4) {
-    if (crpcr1024_applies(a, b, c, d, x, n, m, stride)) return crpcr1024_solve(a, b, c, d, x, m, stride, s);
+    if (crpcr_regs_applies(a, b, c, d, x, n, m, stride)) return crpcr_regs_solve(a, b, c, d, x, n, m, stride, s);
     if (pcr_twophase_applies<T>(p)) {
       const bool paired = tunable(TRIDI_TUNE_PCR_KERNEL) != 3;
       switch (n) {

@@ -49,12 +49,12 @@ long ragged_team_max_rows();
 bool pcr_thomas2_applies(const void* a, const void* b, const void* c, const void* d, int n, long m, int g);
 tridi_status pcr_thomas2_solve(const float* a, const float* b, const float* c, const float* d, float* x, int n,
                                int m, int g, cudaStream_t stream);
-// cr and crpcr at every switch level for 1024 unknowns, in registers
+// cr and crpcr at every switch level for 512 and 1024 unknowns, in registers
 // (crpcr2.cu); stride = n / rest.
-bool crpcr1024_applies(const void* a, const void* b, const void* c, const void* d, const void* x, int n, long m,
-                       int stride);
-tridi_status crpcr1024_solve(const float* a, const float* b, const float* c, const float* d, float* x, int m,
-                             int stride, cudaStream_t stream);
+bool crpcr_regs_applies(const void* a, const void* b, const void* c, const void* d, const void* x, int n, long m,
+                        int stride);
+tridi_status crpcr_regs_solve(const float* a, const float* b, const float* c, const float* d, float* x, int n,
+                              int m, int stride, cudaStream_t stream);
 
 inline int ilog2(long v) {
   int k = 0;
