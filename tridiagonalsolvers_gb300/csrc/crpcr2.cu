@@ -1,10 +1,11 @@
-// CR-PCR for FP32 systems of 1024 unknowns in registers, one system a warp
-// (32 contiguous rows a lane, loaded by TMA into the warp's buffer): every
-// switch level of "crpcr" (restSystemSize 2 .. 512, crpcr_kernel.cu:1-148,
-// crpcr_app.cu:5) and, at rest 2, "cr" (cr_kernel.cu, cr_app.cu:4).
+// CR-PCR for FP32 systems of 1024 (and, in large batches, 512) unknowns in
+// registers, one system a warp (n / 32 contiguous rows a lane, loaded by TMA
+// into the warp's buffer): every switch level of "crpcr" (restSystemSize
+// 2 .. n/2, crpcr_kernel.cu:1-148, crpcr_app.cu:5) and, at rest 2, "cr"
+// (cr_kernel.cu, cr_app.cu:4).
 //
-// crpcr_lanes_kernel<LEV> (rest = 1024 / 2^LEV, LEV = 2 .. 9): the first five
-// CR levels run inside the lane (32 -> 16 -> 8 -> 4 -> 2 -> 1 rows; each level's
+// crpcr_lanes_kernel<N, LEV> (rest = N / 2^LEV): the first log2(N/32) CR
+// levels run inside the lane (32 -> 16 -> 8 -> 4 -> 2 -> 1 rows at N = 1024; each level's
 // last odd row takes its right neighbour from the next lane over one
 // shuffle), the levels past five between lanes (lane strides 1, 2, 4, 8).
 // PCR on the rows left: distances below the rows a lane holds inside the
