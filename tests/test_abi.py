@@ -30,3 +30,14 @@ def test_argument_validation_needs_no_gpu(native):
     assert native.tridi_crpcr_f32(p, p, p, p, p, 256, 4, 3, null) == 2
     assert native.tridi_crpcr_f32(p, p, p, p, p, 256, 4, 256, null) == 2
     assert native.tridi_pcr_f32(p, p, p, p, p, 8192, 4, null) == 2
+
+
+def test_pageable_query_answers_without_a_gpu(native):
+    # 1 only where a device reaches pageable memory through the host's page
+    # tables; with no usable device the answer is 0, not an error.
+    v = native.tridi_dropin_pageable_in_place()
+    assert v in (0, 1)
+    import torch
+
+    if not torch.cuda.is_available():
+        assert v == 0
